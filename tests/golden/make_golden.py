@@ -1,0 +1,212 @@
+"""Regenerate the golden fixtures under tests/golden/cases/.
+
+Each case is a seeded input (FASTA, optional boxes file) plus the CLI
+switches; its expected output is produced by the reference MoTeX itself:
+the unmodified reference sources compiled by oracle/build_ref.sh and linked
+with the libflasm.so shipped in the reference (x86-64 only).  The restated
+oracle (oracle/_build/motex_port) is run on every case as well and must give
+the identical file; a mismatch aborts the script.
+
+The two non-deterministic header lines (``# Rundate:`` and ``# Run on ...``)
+are removed from stored outputs.  Cases run with relative paths (in.fa,
+in.boxes, out.motex) from the case directory, so the header's file lines are
+reproducible.
+
+usage: python tests/golden/make_golden.py   (needs the reference tree and an
+x86-64 host; run oracle/build_ref.sh and make -C oracle first)
+"""
+from __future__ import annotations
+
+import json
+import os
+import shutil
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from motex_gb300 import workloads as W  # noqa: E402
+
+CASES_DIR = os.path.join(HERE, "cases")
+REF = os.path.join(ROOT, "oracle", "_ref")
+PORT = os.path.join(ROOT, "oracle", "_build", "motex_port")
+
+
+def strip_volatile(text: str) -> str:
+    return "".join(l for l in text.splitlines(True)
+                   if not l.startswith("# Rundate:") and not l.startswith("# Run on "))
+
+
+def run_cli(binary, args, cwd):
+    p = subprocess.run([binary] + args, cwd=cwd, capture_output=True, text=True)
+    out = None
+    if os.path.exists(os.path.join(cwd, "out.motex")):
+        with open(os.path.join(cwd, "out.motex")) as f:
+            out = strip_volatile(f.read())
+        os.remove(os.path.join(cwd, "out.motex"))
+    return p.returncode, out
+
+
+# --------------------------------------------------------------- case inputs
+
+def planted_structured(seed, nseq, length, d):
+    """Random DNA with a planted 2-box structured motif (8-mer, gap 5-15,
+    10-mer; <= 1 substitution per box) in half of the sequences."""
+    rng = np.random.default_rng(seed)
+    seqs = [W._rand_seq(rng, W.DNA, length) for _ in range(nseq)]
+    b0, b1 = W._rand_seq(rng, W.DNA, 8), W._rand_seq(rng, W.DNA, 10)
+
+    def copy():
+        gap = W._rand_seq(rng, W.DNA, int(rng.integers(5, 16)))
+        return (W._substitute(rng, b0, W.DNA, int(rng.integers(2))) + gap +
+                W._substitute(rng, b1, W.DNA, int(rng.integers(2))))
+    W._plant(rng, seqs, copy, 0.5)
+    return W.Workload("planted_structured", "DNA", seqs, d=d, k=8, e=1, q=30,
+                      boxes=((5, 15, 10, 1),))
+
+
+def quorum_boundary(seed):
+    """100 sequences; one 10-mer planted exactly in 29 of them and run with
+    q=29: (29/100)*100 evaluates below 29 in IEEE double, so the reference
+    rejects it although 29% of the sequences hold it."""
+    rng = np.random.default_rng(seed)
+    seqs = [W._rand_seq(rng, W.DNA, 40) for _ in range(100)]
+    motif = W._rand_seq(rng, W.DNA, 10)
+    for i in rng.choice(100, size=29, replace=False):
+        pos = int(rng.integers(0, 31))
+        seqs[i] = seqs[i][:pos] + motif + seqs[i][pos + 10:]
+    return W.Workload("quorum_boundary", "DNA", seqs, d=0, k=10, e=0, q=29)
+
+
+def with_n(seed, d):
+    rng = np.random.default_rng(seed)
+    seqs = [W._rand_seq(rng, "ACGTN", int(rng.integers(60, 140)), [0.24, 0.24, 0.24, 0.24, 0.04])
+            for _ in range(16)]
+    return W.Workload("dna_with_N", "DNA", seqs, d=d, k=6, e=1, q=20)
+
+
+def short_seqs(seed, d):
+    rng = np.random.default_rng(seed)
+    lens = [3, 80, 5, 120, 9, 60, 10, 11, 200, 7]
+    seqs = [W._rand_seq(rng, W.DNA, n) for n in lens]
+    return W.Workload("short_seqs", "DNA", seqs, d=d, k=10, e=2, q=10)
+
+
+def usr(seed, d):
+    rng = np.random.default_rng(seed)
+    seqs = [W._rand_seq(rng, "0123456789", int(rng.integers(50, 150))) for _ in range(12)]
+    return W.Workload("usr_digits", "USR", seqs, d=d, k=5, e=1, q=25)
+
+
+def long_factor(seed, d, k, e, nseq=6, length=220):
+    rng = np.random.default_rng(seed)
+    seqs = [W._rand_seq(rng, W.DNA, length) for _ in range(nseq)]
+    src = seqs[0][10:10 + k]
+    for i in range(1, nseq, 2):
+        c = W._edit(rng, src, W.DNA, int(rng.integers(e + 1))) if d else \
+            W._substitute(rng, src, W.DNA, int(rng.integers(e + 1)))
+        seqs[i] = seqs[i][:30] + c + seqs[i][30 + len(c):]
+    return W.Workload(f"long_factor_k{k}", "DNA", seqs, d=d, k=k, e=e, q=30)
+
+
+def raw_fasta_text(seed):
+    """Multi-line records, lower case, an empty record and a header-only record."""
+    rng = np.random.default_rng(seed)
+    seqs = [W._rand_seq(rng, W.DNA, int(rng.integers(40, 90))) for _ in range(6)]
+    txt = ""
+    for i, s in enumerate(seqs):
+        if i == 2:
+            txt += ">empty record\n\n"
+        if i == 4:
+            txt += ">header only\n"
+        body = s.lower() if i % 2 else s
+        txt += f">s{i} description\n" + "\n".join(body[p:p + 25] for p in range(0, len(body), 25)) + "\n"
+    return txt
+
+
+def cases():
+    """(name, workload, extra CLI tokens, raw FASTA text or None)"""
+    out = []
+    out.append(("c1_dna_hd_64x500", W.dna_hd_small(seed=1), [], None))
+    out.append(("dna_ed_24seq", W.dna_ed(seed=2, scale=0.02), [], None))
+    out.append(("dna_hd_24seq", W.dna_ed(seed=2, scale=0.02, d=0), [], None))
+    out.append(("prot_hd_20seq", W.prot_uneven(seed=3, scale=0.01, d=0), [], None))
+    out.append(("prot_ed_20seq", W.prot_uneven(seed=3, scale=0.01, d=1), [], None))
+    out.append(("dna_long_8x2000", W.dna_long(seed=4, scale=0.002), [], None))
+    out.append(("struct_hd_dna_ed_12seq", W.structured(seed=2, scale=0.01, d=0), [], None))
+    out.append(("struct_ed_dna_ed_12seq", W.structured(seed=2, scale=0.01, d=1), [], None))
+    out.append(("struct_planted_hd", planted_structured(11, 16, 150, 0), [], None))
+    out.append(("struct_planted_ed", planted_structured(11, 16, 150, 1), [], None))
+    out.append(("quorum_boundary_q29", quorum_boundary(12), [], None))
+    out.append(("dna_with_N_hd", with_n(13, 0), [], None))
+    out.append(("dna_with_N_ed", with_n(13, 1), [], None))
+    out.append(("short_seqs_hd", short_seqs(14, 0), [], None))
+    out.append(("short_seqs_ed", short_seqs(14, 1), [], None))
+    out.append(("usr_hd", usr(15, 0), [], None))
+    out.append(("usr_ed", usr(15, 1), [], None))
+    w = W.dna_ed(seed=16, scale=0.01, d=0)
+    w.k, w.e, w.q = 6, 1, 0
+    w.n = 0
+    out.append(("q0_n0_all_words", w, [], None))
+    w = W.prot_uneven(seed=17, scale=0.008, d=1)
+    w.k, w.e, w.q, w.Q, w.n, w.N = 5, 1, 10, 60, 2, 40
+    out.append(("caps_Q60_n2_N40", w, [], None))
+    out.append(("long_factor_k40_hd", long_factor(18, 0, 40, 6), [], None))
+    out.append(("long_factor_k40_ed", long_factor(18, 1, 40, 6), [], None))
+    out.append(("long_factor_k70_hd", long_factor(19, 0, 70, 9), [], None))
+    out.append(("long_factor_k70_ed", long_factor(19, 1, 70, 5, nseq=4, length=160), [], None))
+    w = W.Workload("raw_fasta", "DNA", [], d=0, k=5, e=1, q=30)
+    out.append(("raw_fasta_hd", w, [], raw_fasta_text(20)))
+    w = W.dna_ed(seed=21, scale=0.005, d=0)
+    w.k, w.e, w.q = 7, 1, 20
+    out.append(("flag_L_ignored", w, ["-L", "1"], None))
+    return out
+
+
+def main():
+    if not os.path.exists(os.path.join(REF, "motexCPU")):
+        sys.exit("make_golden: oracle/_ref/motexCPU missing (run oracle/build_ref.sh on x86-64)")
+    if not os.path.exists(PORT):
+        sys.exit("make_golden: oracle/_build/motex_port missing (run make -C oracle)")
+    os.makedirs(CASES_DIR, exist_ok=True)
+    for name, w, extra, raw in cases():
+        d = os.path.join(CASES_DIR, name)
+        if os.path.isdir(d):
+            shutil.rmtree(d)
+        os.makedirs(d)
+        if raw is not None:
+            with open(os.path.join(d, "in.fa"), "w") as f:
+                f.write(raw)
+        else:
+            W.write_fasta(os.path.join(d, "in.fa"), w.seqs, width=60)
+        if w.boxes:
+            W.write_boxes(os.path.join(d, "in.boxes"), w.boxes)
+        args = w.cli("in.fa", "out.motex", "in.boxes" if w.boxes else None) + extra
+        big = w.total_len ** 2 * (len(w.boxes) + 1) > 3e8
+        ref_bin = os.path.join(REF, "motexOMP" if big else "motexCPU")
+        ref_args = args + (["-t", str(os.cpu_count())] if big else [])
+        with tempfile.TemporaryDirectory() as tmp:
+            for f in os.listdir(d):
+                shutil.copy(os.path.join(d, f), tmp)
+            rc, ref_out = run_cli(ref_bin, ref_args, tmp)
+            rc2, port_out = run_cli(PORT, args + ["-t", str(os.cpu_count())], tmp)
+        if rc != 0 or ref_out is None:
+            sys.exit(f"make_golden: reference failed on {name} (rc={rc})")
+        if rc2 != rc or port_out != ref_out:
+            sys.exit(f"make_golden: oracle/_build/motex_port disagrees with the reference on {name}")
+        with open(os.path.join(d, "expected.motex"), "w") as f:
+            f.write(ref_out)
+        with open(os.path.join(d, "case.json"), "w") as f:
+            json.dump({"args": args, "reference": os.path.basename(ref_bin),
+                       "motifs": ref_out.count("\n") - ref_out.count("#") - 3}, f, indent=1)
+        print(f"{name:28s} seqs={len(w.seqs) if raw is None else 'raw':>5} "
+              f"lines={ref_out.count(chr(10)):6d} ok")
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,376 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 word-based motif extraction (MoTeX hot path).
+
+Metric: GCUPS = DP cell updates the reference computes (sum over non-skipped
+ordered sequence pairs of m_i * n_j) per second.  One step = one whole-set
+extraction (pack, factor dedup, all-factors x all-texts DP, quorum filter,
+first-occurrence compaction) of the workload.
+
+* value: steps on input already resident in HBM (motex_gpu_execute), device
+  time from CUDA events on the engine's stream; L2 is flushed (256 MiB
+  write) before every timed step.
+* e2e:   the same metric through the public C ABI call motex_gpu_run with
+  host buffers: host->device copy of the sequences, the extraction and the
+  device->host copy of the motif list are inside the timed region.
+* roofline: the factor-search DP kernel against the measured integer-ALU
+  peak (lop3 throughput probe, no vendor figure exists for it).
+* cpu_baseline: the CPU restatement of the reference path (oracle port,
+  OpenMP over all host cores) on a bounded sample of the same workload.
+
+--impl reference times that CPU implementation alone (the reference's own
+libFLASM build is x86-64 only and its sources are not on the GPU host).
+
+usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--workload NAME] [--impl reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import re
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+from motex_gb300 import workloads as W  # noqa: E402
+
+WORKLOADS = {
+    "dna_ed": lambda: W.dna_ed(),
+    "dna_hd_small": lambda: W.dna_hd_small(),
+    "prot_uneven_d0": lambda: W.prot_uneven(d=0),
+    "prot_uneven_d1": lambda: W.prot_uneven(d=1),
+    "dna_long": lambda: W.dna_long(),
+}
+DEFAULT_WORKLOAD = "dna_ed"
+# algorithmic integer operations per DP cell (one factor x one text position)
+OPS_PER_CELL = {0: 6, 1: 17}
+PORT = os.path.join(ROOT, "oracle", "_build", "motex_port")
+REF_OMP = os.path.join(ROOT, "oracle", "_ref", "motexOMP")
+CPU_SAMPLE_SECONDS = 12.0
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+# ---------------------------------------------------------------- CPU side
+
+def ensure_port():
+    if not os.path.exists(PORT):
+        subprocess.run(["make", "-C", os.path.join(ROOT, "oracle"), "-j8"], check=True, capture_output=True)
+
+
+def cpu_binary():
+    """(path, kind): the reference build when it exists on this host, else the port."""
+    if os.path.exists(REF_OMP) and os.access(REF_OMP, os.X_OK):
+        try:
+            subprocess.run([REF_OMP, "-h"], capture_output=True, timeout=10)
+            return REF_OMP, "reference"
+        except OSError:
+            pass
+    ensure_port()
+    return PORT, "port"
+
+
+def cpu_run(binary, wl, seqs, threads):
+    """Run the CPU implementation on seqs; returns (cells, secs) of its own all-pairs timer."""
+    with tempfile.TemporaryDirectory() as tmp:
+        fa, out = os.path.join(tmp, "in.fa"), os.path.join(tmp, "out.motex")
+        W.write_fasta(fa, seqs)
+        args = wl.cli(fa, out) + ["-t", str(threads)]
+        if wl.boxes:
+            bx = os.path.join(tmp, "in.boxes")
+            W.write_boxes(bx, wl.boxes)
+            args[args.index("-s") + 1] = bx
+        p = subprocess.run([binary] + args, capture_output=True, text=True)
+        if p.returncode != 0:
+            raise RuntimeError(f"{binary} failed: {p.stderr[-500:]}")
+        m = re.search(r"# Run on \d+ proc\(s\) in ([0-9.]+) secs", open(out).read())
+        secs = float(m.group(1))
+    tml = wl.k + sum(g[0] + g[2] for g in wl.boxes)
+    searched = sum(len(s) for s in seqs if len(s) >= tml)
+    return searched * searched * (len(wl.boxes) + 1), secs
+
+
+def cpu_sample(binary, wl, threads, target_s=CPU_SAMPLE_SECONDS):
+    """Largest prefix of the workload's sequences that runs in about target_s."""
+    n = max(2, min(len(wl.seqs), 16))
+    while True:
+        cells, secs = cpu_run(binary, wl, wl.seqs[:n], threads)
+        if n >= len(wl.seqs) or secs >= target_s / 4:
+            break
+        n = min(len(wl.seqs), max(n + 1, int(n * 2)))
+    # cost grows ~ quadratically in the number of sequences
+    scale = (target_s / max(secs, 1e-3)) ** 0.5
+    n2 = max(2, min(len(wl.seqs), int(n * scale)))
+    return wl.seqs[:n2]
+
+
+# ---------------------------------------------------------------- clocks
+
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+        sm, smax, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = max(smax, float(f[2]))
+            except ValueError:
+                continue
+            for name, val in zip(names, f[5:9]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ---------------------------------------------------------------- GPU side
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f)
+    except OSError:
+        return {}
+
+
+def traffic_record(workload):
+    """DRAM bytes per DP launch from the committed ncu summary, if any."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "dp_traffic.json")) as f:
+            rec = json.load(f)
+        return rec.get(workload)
+    except (OSError, ValueError):
+        return None
+
+
+def run_gpu(args, rank, world, local_rank):
+    import ctypes as C
+    import torch
+    from motex_gb300 import native
+
+    torch.cuda.set_device(local_rank)
+    wl = WORKLOADS[args.workload]()
+    prm = native.make_params(wl.d, wl.k, wl.e, wl.q, wl.Q, wl.n, wl.N, wl.boxes)
+    ctx = native.Context(local_rank)
+    lib = ctx.lib
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{local_rank}")
+
+    def dist_barrier():
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    # ---- value: device-resident steps
+    ctx.load(wl.seqs, prm)
+    for _ in range(args.warmup):
+        ctx.execute()
+    first = ctx.fetch()
+    dist_barrier()
+    torch.cuda.synchronize()
+    sampler = ClockSampler(local_rank)
+    sampler.start()
+    launches0 = ctx.launches
+    dev_ms, dp_ms, wall = [], [], []
+    results = []
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ctx.execute()
+        wall.append(time.perf_counter() - t0)
+        r = ctx.fetch()
+        dev_ms.append(r.device_ms)
+        dp_ms.append(r.dp_ms)
+        results.append(r.motifs)
+    launches = ctx.launches - launches0
+    torch.cuda.synchronize()
+    dist_barrier()
+    clocks = sampler.stop()
+    assert all(m == first.motifs for m in results), "non-deterministic result across steps"
+
+    # ---- e2e: public C ABI with host buffers
+    bs = [s.encode() for s in wl.seqs]
+    arr = (C.c_char_p * len(bs))(*bs)
+    lens = (C.c_uint32 * len(bs))(*[len(b) for b in bs])
+    res = native.Result()
+    e2e_wall = []
+    for i in range(args.warmup + args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        rc = lib.motex_gpu_run(ctx.h, C.byref(prm), arr, lens, len(bs), C.byref(res))
+        dt = time.perf_counter() - t0
+        if rc != 0:
+            raise native.MotexError(rc, lib.motex_gpu_last_error().decode())
+        count = res.count
+        lib.motex_result_free(C.byref(res))
+        if i >= args.warmup:
+            e2e_wall.append(dt)
+    assert count == len(first.motifs)
+
+    total = sum(len(b) for b in bs)
+    h2d = total + 2 * 4 * (len(bs) + 1) + (len(bs) + 1) + 256
+    d2h = 12 * count + 256 * 4 + 8
+
+    # ---- aggregate over ranks (replicas)
+    step_s = max(sum(dev_ms) / 1e3, 1e-9)
+    e2e_s = max(sum(e2e_wall), 1e-9)
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([step_s, e2e_s], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        step_s, e2e_s = float(t[0]), float(t[1])
+    cells = first.ref_cells
+    value = cells * args.steps * world / step_s / 1e9
+    e2e = cells * args.steps * world / e2e_s / 1e9
+
+    # ---- roofline of the DP kernel
+    lop3, iadd, popc = native.probe_int_peak(local_rank)
+    total_pos = sum(len(s) for s in wl.seqs)
+    alg_ops = first.unique_words * total_pos * OPS_PER_CELL[wl.d]
+    dp_s = statistics.mean(dp_ms) / 1e3
+    achieved = alg_ops / dp_s / 1e12 if dp_s > 0 else 0.0
+    tr = traffic_record(args.workload)
+    roofline = {"bound": "int32_alu", "kernel": "k_dp_fast", "achieved": round(achieved, 3),
+                "peak": round(lop3, 3), "unit": "Tops/s", "frac": round(achieved / lop3, 4) if lop3 else None,
+                "peak_source": "measured lop3 throughput probe (motex_probe_int_peak), same run",
+                "iadd_peak": round(iadd, 3), "popc_peak": round(popc, 3),
+                "ops_per_cell": OPS_PER_CELL[wl.d], "cells_per_launch": first.unique_words * total_pos,
+                "dp_ms": round(dp_s * 1e3, 3), "traffic": tr}
+
+    out = {
+        "metric": "GCUPS (reference DP cell updates per second), whole-set word-based motif extraction",
+        "value": round(value, 2), "unit": "GCUPS", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(step_s * 1e3 / args.steps, 3), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u32 bit-vector (integer)", "data": "synthetic (seeded generator)",
+        "config": {"workload": args.workload, "alphabet": wl.alphabet, "num_seqs": len(wl.seqs),
+                   "total_len": total_pos, "d": wl.d, "k": wl.k, "e": wl.e, "q": wl.q,
+                   "ref_cells": cells, "unique_words": first.unique_words, "motifs": len(first.motifs),
+                   "parallelism": f"replicas{world}", "l2": "flushed (256 MiB write) before every step",
+                   "host_wall_ms_per_step": round(1e3 * statistics.mean(wall), 3)},
+        "e2e": {"value": round(e2e, 2), "unit": "GCUPS", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "ms_per_step": round(e2e_s * 1e3 / args.steps, 3)},
+        "gpu_launches": launches,
+        "roofline": roofline,
+        "clocks": clocks,
+        "measured_peaks": {k: measured_peaks().get(k) for k in ("hbm_gbs", "bf16_tflops")},
+    }
+    ctx.close()
+    return out, wl
+
+
+def run_reference(args):
+    """Reference arm: the CPU implementation of the path, all host threads."""
+    wl = WORKLOADS[args.workload]()
+    binary, kind = cpu_binary()
+    threads = os.cpu_count() or 1
+    sample = cpu_sample(binary, wl, threads, target_s=8.0)
+    for _ in range(args.warmup):
+        cpu_run(binary, wl, sample, threads)
+    cells_t, secs_t = 0, 0.0
+    for _ in range(args.steps):
+        c, s = cpu_run(binary, wl, sample, threads)
+        cells_t += c
+        secs_t += s
+    val = cells_t / secs_t / 1e9
+    desc = f"first {len(sample)} of {len(wl.seqs)} sequences ({sum(map(len, sample))} symbols)"
+    return {
+        "impl": "reference", "metric": "GCUPS (reference DP cell updates per second), whole-set word-based motif extraction",
+        "value": round(val, 3), "unit": "GCUPS", "n_gpus": 0, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(secs_t * 1e3 / args.steps, 3), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "integer", "data": "synthetic (seeded generator)",
+        "config": {"workload": args.workload, "alphabet": wl.alphabet, "d": wl.d, "k": wl.k, "e": wl.e, "q": wl.q},
+        "cpu_baseline": {"value": round(val, 3), "unit": "GCUPS", "cores": threads, "kind": kind, "sample": desc},
+        "e2e": {"value": round(val, 3), "unit": "GCUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS))
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+
+    if args.impl == "reference":
+        if rank == 0:
+            print(json.dumps(run_reference(args)), flush=True)
+        return
+
+    if world > 1:
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group("gloo", rank=rank, world_size=world)
+    out, wl = run_gpu(args, rank, world, local_rank)
+    if rank == 0:
+        if not args.no_cpu_baseline:
+            binary, kind = cpu_binary()
+            threads = os.cpu_count() or 1
+            sample = cpu_sample(binary, wl, threads)
+            cells, secs = cpu_run(binary, wl, sample, threads)
+            out["cpu_baseline"] = {"value": round(cells / secs / 1e9, 3), "unit": "GCUPS", "cores": threads,
+                                   "kind": kind,
+                                   "sample": f"first {len(sample)} of {len(wl.seqs)} sequences, {secs:.1f} s"}
+        print(json.dumps(out), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

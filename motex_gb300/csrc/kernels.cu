@@ -1,0 +1,428 @@
+// Packing, factor deduplication (stable LSD radix sort), filter and
+// compaction kernels of the GB300 motif-extraction engine.
+#include "kernels.cuh"
+
+namespace mtx
+{
+
+// ------------------------------------------------------------------ scans
+
+// Exclusive scan of one value per thread across a CTA of kScanThreads.
+__device__ __forceinline__ uint32_t block_exclusive_scan ( uint32_t v, uint32_t * total )
+{
+    __shared__ uint32_t warp_sums[32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t x = v;
+#pragma unroll
+    for ( int o = 1; o < 32; o <<= 1 )
+    {
+        uint32_t y = __shfl_up_sync ( 0xffffffffu, x, o );
+        if ( lane >= o ) x += y;
+    }
+    if ( lane == 31 ) warp_sums[warp] = x;
+    __syncthreads ();
+    if ( warp == 0 )
+    {
+        const int nw = blockDim.x >> 5;
+        uint32_t s = lane < nw ? warp_sums[lane] : 0u;
+#pragma unroll
+        for ( int o = 1; o < 32; o <<= 1 )
+        {
+            uint32_t y = __shfl_up_sync ( 0xffffffffu, s, o );
+            if ( lane >= o ) s += y;
+        }
+        warp_sums[lane] = s;           // inclusive warp-sum prefix
+    }
+    __syncthreads ();
+    const uint32_t before = warp ? warp_sums[warp - 1] : 0u;
+    if ( total ) *total = warp_sums[( blockDim.x >> 5 ) - 1];
+    __syncthreads ();
+    return before + x - v;
+}
+
+// In-place exclusive scan of n words with a single CTA; *total = sum.
+__global__ void __launch_bounds__ ( kScanThreads ) k_scan_single ( uint32_t * data, uint32_t n, uint32_t * total )
+{
+    const uint32_t seg = ( n + kScanThreads - 1 ) / kScanThreads;
+    const uint32_t s0 = min ( n, threadIdx.x * seg ), s1 = min ( n, s0 + seg );
+    uint32_t sum = 0;
+    for ( uint32_t i = s0; i < s1; ++i ) sum += data[i];
+    uint32_t tot;
+    uint32_t run = block_exclusive_scan ( sum, &tot );
+    for ( uint32_t i = s0; i < s1; ++i )
+    {
+        uint32_t v = data[i];
+        data[i] = run;
+        run += v;
+    }
+    if ( threadIdx.x == 0 && total ) *total = tot;
+}
+
+template <typename T>
+__global__ void __launch_bounds__ ( kScanThreads ) k_tile_reduce ( const T * in, uint32_t n, uint32_t * tile_sums )
+{
+    const uint32_t base = blockIdx.x * kScanTile;
+    uint32_t s = 0;
+#pragma unroll
+    for ( int r = 0; r < kScanItems; ++r )
+    {
+        uint32_t i = base + r * kScanThreads + threadIdx.x;
+        if ( i < n ) s += ( uint32_t ) in[i];
+    }
+    uint32_t tot;
+    block_exclusive_scan ( s, &tot );
+    if ( threadIdx.x == 0 ) tile_sums[blockIdx.x] = tot;
+}
+
+template <typename T>
+__global__ void __launch_bounds__ ( kScanThreads ) k_tile_scan ( const T * in, uint32_t n, const uint32_t * tile_off,
+                                                                  uint32_t * out )
+{
+    // thread t owns kScanItems consecutive items so the output order is preserved
+    const uint32_t base = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
+    uint32_t v[kScanItems];
+    uint32_t s = 0;
+#pragma unroll
+    for ( int r = 0; r < kScanItems; ++r )
+    {
+        uint32_t i = base + r;
+        v[r] = i < n ? ( uint32_t ) in[i] : 0u;
+        s += v[r];
+    }
+    uint32_t run = tile_off[blockIdx.x] + block_exclusive_scan ( s, nullptr );
+#pragma unroll
+    for ( int r = 0; r < kScanItems; ++r )
+    {
+        uint32_t i = base + r;
+        if ( i < n ) out[i] = run;
+        run += v[r];
+    }
+}
+
+template <typename T>
+static cudaError_t scan_exclusive_impl ( const T * in, uint32_t n, uint32_t * out, uint32_t * d_total,
+                                         uint32_t * tile_sums, cudaStream_t st )
+{
+    const uint32_t tiles = ( n + kScanTile - 1 ) / kScanTile;
+    k_tile_reduce<T><<<tiles ? tiles : 1, kScanThreads, 0, st>>> ( in, n, tile_sums );
+    k_scan_single<<<1, kScanThreads, 0, st>>> ( tile_sums, tiles ? tiles : 1, d_total );
+    k_tile_scan<T><<<tiles ? tiles : 1, kScanThreads, 0, st>>> ( in, n, tile_sums, out );
+    return cudaGetLastError ();
+}
+
+cudaError_t scan_exclusive_u8 ( const uint8_t * in, uint32_t n, uint32_t * out, uint32_t * d_total,
+                                uint32_t * tile_sums, cudaStream_t st )
+{
+    return scan_exclusive_impl<uint8_t> ( in, n, out, d_total, tile_sums, st );
+}
+
+cudaError_t scan_exclusive_u32 ( const uint32_t * in, uint32_t n, uint32_t * out, uint32_t * d_total,
+                                 uint32_t * tile_sums, cudaStream_t st )
+{
+    return scan_exclusive_impl<uint32_t> ( in, n, out, d_total, tile_sums, st );
+}
+
+// ------------------------------------------------------------------ packing
+
+// present[c] = 1 for every byte value c occurring in raw[0..total).
+__global__ void k_presence ( const uint8_t * __restrict__ raw, uint64_t total, uint32_t * present )
+{
+    __shared__ uint32_t seen[256];
+    for ( int i = threadIdx.x; i < 256; i += blockDim.x ) seen[i] = 0;
+    __syncthreads ();
+    const uint64_t stride = ( uint64_t ) gridDim.x * blockDim.x * 16;
+    for ( uint64_t p = ( ( uint64_t ) blockIdx.x * blockDim.x + threadIdx.x ) * 16; p < total; p += stride )
+    {
+        if ( p + 16 <= total && ( ( ( uintptr_t ) ( raw + p ) ) & 15 ) == 0 )
+        {
+            uint4 q = *reinterpret_cast<const uint4 *> ( raw + p );
+            uint32_t w[4] = { q.x, q.y, q.z, q.w };
+#pragma unroll
+            for ( int j = 0; j < 4; ++j )
+#pragma unroll
+                for ( int b = 0; b < 4; ++b ) seen[( w[j] >> ( 8 * b ) ) & 255] = 1;
+        }
+        else
+            for ( uint64_t i = p; i < min ( total, p + 16 ); ++i ) seen[raw[i]] = 1;
+    }
+    __syncthreads ();
+    for ( int i = threadIdx.x; i < 256; i += blockDim.x )
+        if ( seen[i] ) present[i] = 1;
+}
+
+/*
+ * One warp per 32-position block (grid-stride).  Lane r maps position
+ * 32k+r to its symbol code, finds its sequence, and the warp forms the bit
+ * planes, validity and end masks with ballots.  Also writes the position of
+ * every factor end (in input order) to wpos.
+ */
+__global__ void k_pack ( PackArgs a )
+{
+    __shared__ uint8_t cmap[256];
+    for ( int i = threadIdx.x; i < 256; i += blockDim.x ) cmap[i] = a.cmap[i];
+    __syncthreads ();
+    const int lane = threadIdx.x & 31;
+    const uint32_t warps = ( gridDim.x * blockDim.x ) >> 5;
+    for ( uint32_t k = ( blockIdx.x * blockDim.x + threadIdx.x ) >> 5; k < a.nblk; k += warps )
+    {
+        const uint64_t pos = ( uint64_t ) k * 32 + lane;
+        uint32_t code = 0;
+        bool valid = false, is_end = false;
+        if ( pos < a.total )
+        {
+            // largest s with offs[s] <= pos (lane 0 searches, the rest walk forward)
+            uint32_t s = 0;
+            if ( lane == 0 )
+            {
+                uint32_t lo = 0, hi = a.nseq;                 // offs[lo] <= pos < offs[hi]
+                while ( hi - lo > 1 )
+                {
+                    uint32_t mid = ( lo + hi ) >> 1;
+                    if ( a.offs[mid] <= pos ) lo = mid; else hi = mid;
+                }
+                s = lo;
+            }
+            s = __shfl_sync ( __activemask (), s, 0 );
+            while ( a.offs[s + 1] <= pos ) ++s;
+            const uint64_t start = a.offs[s], end = a.offs[s + 1];
+            const uint64_t rel = pos - start;
+            const bool is_short = ( end - start ) < a.tml;
+            code = cmap[a.raw[pos]];
+            a.codes[pos] = ( uint8_t ) code;
+            // pair mode: sequence 0 is the pattern sequence (factors only),
+            // sequence 1 the text (searched only)
+            valid = ! is_short && rel >= a.vstart && ! ( a.pair_mode && s == 0 );
+            is_end = pos == end - 1;
+            if ( ! is_short && rel + 1 >= a.l && ( ! a.pair_mode || s == 0 ) )
+                a.wpos[a.wstart[s] + ( uint32_t ) ( rel + 1 - a.l )] = ( uint32_t ) pos;
+        }
+        const uint32_t full = 0xffffffffu;
+#pragma unroll
+        for ( int b = 0; b < kMaxPlanes; ++b )
+        {
+            if ( b >= a.B ) break;
+            uint32_t pl = __ballot_sync ( full, ( code >> b ) & 1u );
+            if ( lane == 0 ) a.planes[( size_t ) b * a.plane_stride + k + 1] = pl;
+        }
+        uint32_t vm = __ballot_sync ( full, valid ), em = __ballot_sync ( full, is_end );
+        if ( lane == 0 )
+        {
+            a.vmask[k] = vm;
+            a.emask[k] = em;
+        }
+    }
+}
+
+// ------------------------------------------------------------------ dedup
+
+// key_out[i] = bits [lo, lo+32) of the packed factor ending at idx[i]
+// (first symbol most significant, B bits per symbol).
+__global__ void k_gather_key ( const uint32_t * __restrict__ idx, uint32_t n, const uint8_t * __restrict__ codes,
+                               uint32_t l, uint32_t B, uint32_t lo, uint32_t * __restrict__ key_out )
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if ( i >= n ) return;
+    const uint32_t p = idx[i];
+    const uint32_t e0 = lo / B, e1 = min ( l - 1, ( lo + 31 ) / B );
+    uint64_t acc = 0;
+    for ( uint32_t e = e0; e <= e1; ++e )
+    {
+        const uint64_t c = codes[p - e];
+        const int sh = ( int ) ( e * B ) - ( int ) lo;
+        acc |= sh >= 0 ? ( c << sh ) : ( c >> ( -sh ) );
+    }
+    key_out[i] = ( uint32_t ) acc;
+}
+
+// Per-tile digit histogram, digit-major: hist[d * ntiles + tile].
+__global__ void __launch_bounds__ ( kSortThreads ) k_radix_hist ( const uint32_t * __restrict__ keys, uint32_t n,
+                                                                   int shift, uint32_t * hist, uint32_t ntiles )
+{
+    __shared__ uint32_t cnt[256];
+    for ( int d = threadIdx.x; d < 256; d += kSortThreads ) cnt[d] = 0;
+    __syncthreads ();
+    const uint32_t base = blockIdx.x * kSortTile;
+#pragma unroll 4
+    for ( int r = 0; r < kSortItems; ++r )
+    {
+        uint32_t i = base + r * kSortThreads + threadIdx.x;
+        if ( i < n ) atomicAdd ( &cnt[( keys[i] >> shift ) & 255u], 1u );
+    }
+    __syncthreads ();
+    for ( int d = threadIdx.x; d < 256; d += kSortThreads ) hist[( size_t ) d * ntiles + blockIdx.x] = cnt[d];
+}
+
+/*
+ * Stable scatter of one 8-bit digit.  Items are visited in input order
+ * (round r, then thread index); ranks among equal digits come from warp
+ * match masks plus per-warp counts, so equal keys keep their order.
+ */
+__global__ void __launch_bounds__ ( kSortThreads ) k_radix_scatter ( const uint32_t * __restrict__ keys_in,
+                                                                      const uint32_t * __restrict__ vals_in,
+                                                                      uint32_t * __restrict__ keys_out,
+                                                                      uint32_t * __restrict__ vals_out,
+                                                                      uint32_t n, int shift,
+                                                                      const uint32_t * __restrict__ offsets,
+                                                                      uint32_t ntiles )
+{
+    constexpr int NW = kSortThreads / 32;
+    __shared__ uint32_t s_base[256];
+    __shared__ uint32_t s_run[256];
+    __shared__ uint32_t s_wcnt[NW][256];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for ( int d = threadIdx.x; d < 256; d += kSortThreads )
+    {
+        s_base[d] = offsets[( size_t ) d * ntiles + blockIdx.x];
+        s_run[d] = 0;
+#pragma unroll
+        for ( int w = 0; w < NW; ++w ) s_wcnt[w][d] = 0;
+    }
+    __syncthreads ();
+    const uint32_t base = blockIdx.x * kSortTile;
+    const uint32_t lt = lanemask_lt ();
+    for ( int r = 0; r < kSortItems; ++r )
+    {
+        const uint32_t i = base + r * kSortThreads + threadIdx.x;
+        const bool valid = i < n;
+        const uint32_t k = valid ? keys_in[i] : 0u;
+        const uint32_t v = valid ? vals_in[i] : 0u;
+        const uint32_t d = valid ? ( ( k >> shift ) & 255u ) : ( 256u + lane );
+        const uint32_t peers = __match_any_sync ( 0xffffffffu, d );
+        const uint32_t rank = __popc ( peers & lt );
+        if ( valid && rank == 0 ) s_wcnt[warp][d] = __popc ( peers );
+        __syncthreads ();
+        if ( valid )
+        {
+            uint32_t off = s_run[d];
+            for ( int w = 0; w < warp; ++w ) off += s_wcnt[w][d];
+            const uint32_t dst = s_base[d] + off + rank;
+            keys_out[dst] = k;
+            vals_out[dst] = v;
+        }
+        __syncthreads ();
+        for ( int dd = threadIdx.x; dd < 256; dd += kSortThreads )
+        {
+            uint32_t t = 0;
+#pragma unroll
+            for ( int w = 0; w < NW; ++w )
+            {
+                t += s_wcnt[w][dd];
+                s_wcnt[w][dd] = 0;
+            }
+            s_run[dd] += t;
+        }
+        __syncthreads ();
+    }
+}
+
+// head[i] = 1 iff the factor at idx[i] differs from the one at idx[i-1].
+__global__ void k_heads ( const uint32_t * __restrict__ idx, uint32_t n, const uint8_t * __restrict__ codes,
+                          uint32_t l, uint8_t * __restrict__ head )
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if ( i >= n ) return;
+    uint8_t h = 1;
+    if ( i > 0 )
+    {
+        const uint32_t p = idx[i], q = idx[i - 1];
+        h = 0;
+        for ( uint32_t e = 0; e < l; ++e )
+            if ( codes[p - e] != codes[q - e] ) { h = 1; break; }
+    }
+    head[i] = h;
+}
+
+__global__ void k_unique ( const uint32_t * __restrict__ idx, const uint8_t * __restrict__ head,
+                           const uint32_t * __restrict__ pref, uint32_t n, uint32_t * __restrict__ uniq_pos )
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if ( i < n && head[i] ) uniq_pos[pref[i]] = idx[i];
+}
+
+/*
+ * Bit planes of each searched factor (factor ends at uniq_pos[w]).
+ * Hamming fast kernel: symbol q at bit 32-l+q (top-aligned, matching text
+ * windows whose newest symbol is bit 31).  Edit distance: symbol q at bit q.
+ */
+__global__ void k_wplanes32 ( const uint32_t * __restrict__ uniq_pos, uint32_t U, const uint8_t * __restrict__ codes,
+                              uint32_t l, uint32_t B, int top_aligned, uint32_t * __restrict__ out )
+{
+    const uint32_t w = blockIdx.x * blockDim.x + threadIdx.x;
+    if ( w >= U ) return;
+    const uint32_t first = uniq_pos[w] + 1 - l;
+    uint32_t pl[kMaxPlanes] = { 0, 0, 0, 0, 0 };
+    for ( uint32_t q = 0; q < l; ++q )
+    {
+        const uint32_t c = codes[first + q];
+        const uint32_t bit = top_aligned ? ( 32 - l + q ) : q;
+#pragma unroll
+        for ( int b = 0; b < kMaxPlanes; ++b ) pl[b] |= ( ( c >> b ) & 1u ) << bit;
+    }
+    for ( uint32_t b = 0; b < B; ++b ) out[( size_t ) b * U + w] = pl[b];
+}
+
+/*
+ * 64-bit multiword planes for the generic kernel (any l <= MOTEX_MAX_FACTOR).
+ * Edit distance: symbol q at bit q.  Hamming: symbol q at bit l-1-q (the
+ * newest text symbol enters the sliding window at bit 0).
+ */
+__global__ void k_wplanes64 ( const uint32_t * __restrict__ uniq_pos, uint32_t U, const uint8_t * __restrict__ codes,
+                              uint32_t l, uint32_t B, uint32_t nw64, int reversed, uint64_t * __restrict__ out )
+{
+    const uint32_t w = blockIdx.x * blockDim.x + threadIdx.x;
+    if ( w >= U ) return;
+    const uint32_t first = uniq_pos[w] + 1 - l;
+    for ( uint32_t b = 0; b < B; ++b )
+        for ( uint32_t j = 0; j < nw64; ++j )
+        {
+            uint64_t word = 0;
+            for ( uint32_t bit = 0; bit < 64; ++bit )
+            {
+                const uint32_t g = j * 64 + bit;             // bit index inside the factor
+                if ( g >= l ) break;
+                const uint32_t q = reversed ? ( l - 1 - g ) : g;
+                word |= ( uint64_t ) ( ( codes[first + q] >> b ) & 1u ) << bit;
+            }
+            out[( ( size_t ) b * U + w ) * nw64 + j] = word;
+        }
+}
+
+// ------------------------------------------------------------------ filter
+
+/*
+ * Quorum filter of functions.cc:1105-1108 (qok[u] holds the reference's
+ * double-precision quorum test for u sequences, computed on the host) and
+ * first-occurrence marking: each searched factor passing the filter is
+ * reported at its first occurrence.
+ */
+__global__ void k_finalize ( FinalizeArgs a )
+{
+    const uint32_t w = blockIdx.x * blockDim.x + threadIdx.x;
+    if ( w >= a.U ) return;
+    uint32_t u = a.u_acc[w];
+    for ( uint32_t s = 0; s < a.n_split; ++s ) u += a.split_flags[( size_t ) s * a.U + w];
+    const uint32_t v = a.v_acc[w];
+    if ( a.u_out ) { a.u_out[w] = u; a.v_out[w] = v; }
+    if ( ! a.mark ) return;
+    if ( u <= a.nseq && a.qok[u] && v >= a.nmin && v <= a.nmax )
+    {
+        const uint32_t p = a.uniq_pos[w];
+        a.mark[p] = 1;
+        a.rec_u[p] = u;
+        a.rec_v[p] = v;
+    }
+}
+
+__global__ void k_compact ( const uint8_t * __restrict__ mark, const uint32_t * __restrict__ pref, uint32_t n,
+                            const uint32_t * __restrict__ rec_u, const uint32_t * __restrict__ rec_v,
+                            uint32_t * __restrict__ out )
+{
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if ( p >= n || ! mark[p] ) return;
+    const uint32_t j = pref[p];
+    out[3 * ( size_t ) j + 0] = p;
+    out[3 * ( size_t ) j + 1] = rec_u[p];
+    out[3 * ( size_t ) j + 2] = rec_v[p];
+}
+
+} // namespace mtx

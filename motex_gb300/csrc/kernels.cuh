@@ -1,0 +1,81 @@
+// Kernel declarations and argument blocks of the GB300 motif-extraction engine.
+#pragma once
+
+#include "common.cuh"
+
+namespace mtx
+{
+
+constexpr int kScanItems = 4;
+constexpr int kScanTile = kScanThreads * kScanItems;
+
+struct PackArgs
+{
+    const uint8_t *  raw;          // concatenated sequences
+    uint64_t         total;
+    const uint32_t * offs;         // nseq + 1 sequence offsets
+    uint32_t         nseq;
+    const uint8_t *  cmap;         // byte -> symbol code
+    int              B;            // bit planes
+    uint32_t         l;            // factor length (box 0)
+    uint32_t         tml;          // minimum sequence length (shorter ones are skipped)
+    uint32_t         vstart;       // first position (relative) at which a match may end
+    int              pair_mode;
+    const uint32_t * wstart;       // first factor index of each sequence
+    uint8_t *        codes;
+    uint32_t *       planes;
+    uint32_t         plane_stride;
+    uint32_t *       vmask;
+    uint32_t *       emask;
+    uint32_t *       wpos;
+    uint32_t         nblk;
+};
+
+struct FinalizeArgs
+{
+    uint32_t          U;
+    const uint32_t *  u_acc;
+    const uint32_t *  v_acc;
+    const uint8_t *   split_flags;
+    uint32_t          n_split;
+    const uint8_t *   qok;           // nseq + 1 entries
+    uint32_t          nseq;
+    uint32_t          nmin, nmax;
+    const uint32_t *  uniq_pos;
+    uint8_t *         mark;        // null: only write u_out / v_out
+    uint32_t *        rec_u;
+    uint32_t *        rec_v;
+    uint32_t *        u_out;       // optional per-factor totals
+    uint32_t *        v_out;
+};
+
+__global__ void k_scan_single ( uint32_t * data, uint32_t n, uint32_t * total );
+// Exclusive scans (3 launches each); tile_sums holds ceil(n / kScanTile) words.
+cudaError_t scan_exclusive_u8 ( const uint8_t * in, uint32_t n, uint32_t * out, uint32_t * d_total,
+                                uint32_t * tile_sums, cudaStream_t st );
+cudaError_t scan_exclusive_u32 ( const uint32_t * in, uint32_t n, uint32_t * out, uint32_t * d_total,
+                                 uint32_t * tile_sums, cudaStream_t st );
+
+__global__ void k_presence ( const uint8_t * raw, uint64_t total, uint32_t * present );
+__global__ void k_pack ( PackArgs a );
+__global__ void k_gather_key ( const uint32_t * idx, uint32_t n, const uint8_t * codes, uint32_t l, uint32_t B,
+                               uint32_t lo, uint32_t * key_out );
+__global__ void k_radix_hist ( const uint32_t * keys, uint32_t n, int shift, uint32_t * hist, uint32_t ntiles );
+__global__ void k_radix_scatter ( const uint32_t * keys_in, const uint32_t * vals_in, uint32_t * keys_out,
+                                  uint32_t * vals_out, uint32_t n, int shift, const uint32_t * offsets, uint32_t ntiles );
+__global__ void k_heads ( const uint32_t * idx, uint32_t n, const uint8_t * codes, uint32_t l, uint8_t * head );
+__global__ void k_unique ( const uint32_t * idx, const uint8_t * head, const uint32_t * pref, uint32_t n,
+                           uint32_t * uniq_pos );
+__global__ void k_wplanes32 ( const uint32_t * uniq_pos, uint32_t U, const uint8_t * codes, uint32_t l, uint32_t B,
+                              int top_aligned, uint32_t * out );
+__global__ void k_wplanes64 ( const uint32_t * uniq_pos, uint32_t U, const uint8_t * codes, uint32_t l, uint32_t B,
+                              uint32_t nw64, int reversed, uint64_t * out );
+__global__ void k_finalize ( FinalizeArgs a );
+__global__ void k_compact ( const uint8_t * mark, const uint32_t * pref, uint32_t n, const uint32_t * rec_u,
+                            const uint32_t * rec_v, uint32_t * out );
+
+// DP launchers (dp.cu): return false if no kernel matches the shape.
+bool launch_dp_fast ( const DPArgs & a, int B, int W, bool ed, dim3 grid, cudaStream_t st );
+bool launch_dp_generic ( const DPArgs & a, int B, uint32_t nw64, bool ed, dim3 grid, cudaStream_t st );
+
+} // namespace mtx

@@ -1,0 +1,110 @@
+"""The oracle (CPU restatement) against the reference's own outputs.
+
+* golden fixtures: outputs of the reference MoTeX itself (its sources
+  compiled with g++, linked to the shipped libflasm.so), regenerated by
+  tests/golden/make_golden.py;
+* the restated flasm against the shipped libflasm.so (x86-64 only);
+* the edit-distance / Hamming cores against brute force on small cases.
+"""
+import ctypes as C
+import os
+import platform
+import random
+import subprocess
+
+import pytest
+
+from conftest import ORACLE_DIR, PORT_LIB, ROOT, golden_cases
+from helpers import load_case, run_cli
+
+REFERENCE = "/root/reference"
+
+
+@pytest.mark.parametrize("name", golden_cases())
+def test_port_matches_reference_golden(oracle_port, name):
+    d, args, expected = load_case(name)
+    rc, out, err = run_cli(oracle_port, d, args, extra=["-t", "4"])
+    assert rc == 0, err
+    assert out == expected
+
+
+def test_golden_set_is_complete():
+    names = set(golden_cases())
+    for needed in ("c1_dna_hd_64x500", "dna_ed_24seq", "prot_hd_20seq", "prot_ed_20seq", "struct_planted_hd",
+                   "struct_planted_ed", "quorum_boundary_q29", "dna_with_N_ed", "short_seqs_ed",
+                   "long_factor_k70_ed", "q0_n0_all_words", "caps_Q60_n2_N40"):
+        assert needed in names
+
+
+def _difftest_binary():
+    b = os.path.join(ORACLE_DIR, "_ref", "flasm_difftest")
+    if not os.path.exists(b) and os.path.isdir(REFERENCE):
+        subprocess.run([os.path.join(ORACLE_DIR, "build_ref.sh"), REFERENCE], check=True, capture_output=True)
+    return b
+
+
+@pytest.mark.skipif(platform.machine() != "x86_64", reason="the shipped libflasm.so is x86-64 only")
+def test_flasm_port_vs_shipped_library():
+    b = _difftest_binary()
+    if not os.path.exists(b):
+        pytest.skip("reference tree not available on this host")
+    for seed, mode in ((11, []), (12, ["edge"])):
+        p = subprocess.run([b, "1500", str(seed)] + mode, capture_output=True, text=True, timeout=300)
+        assert p.returncode == 0 and p.stdout.startswith("OK"), p.stdout + p.stderr
+
+
+# ---------------------------------------------------------------- brute force
+
+def _ed_end(w, t, i):
+    """min_s EditDistance(w, t[s..i]) (empty t-factor allowed)."""
+    l = len(w)
+    col = list(range(l + 1))
+    best = col[l]
+    for ch in t[: i + 1]:
+        nxt = [0] * (l + 1)
+        for p in range(1, l + 1):
+            nxt[p] = min(col[p - 1] + (w[p - 1] != ch), col[p] + 1, nxt[p - 1] + 1)
+        col = nxt
+    return col[l]
+
+
+def brute_pair(d, l, e, p, t):
+    """u/v contributions of one (pattern p, text t) pair, flasm contract."""
+    m = len(p)
+    u, v = [0] * m, [0] * m
+    for j in range(l - 1, m):
+        w = p[j - l + 1: j + 1]
+        hits = 0
+        if d == 0:
+            for i in range(l - 1, len(t)):
+                if sum(a != b for a, b in zip(w, t[i - l + 1: i + 1])) <= e:
+                    hits += 1
+        else:
+            for i in range(len(t)):
+                if _ed_end(w, t, i) <= e:
+                    hits += 1
+        u[j] += hits > 0
+        v[j] += hits
+    return u, v
+
+
+def port_pair(d, l, e, p, t):
+    lib = C.CDLL(PORT_LIB)
+    m = len(p)
+    U = (C.c_uint32 * m)()
+    V = (C.c_uint32 * m)()
+    lib.oracle_extract_pair(d, l, e, p.encode(), m, t.encode(), len(t), U, V)
+    return list(U), list(V)
+
+
+@pytest.mark.parametrize("d", [0, 1])
+def test_port_pair_vs_bruteforce(oracle_port, d):
+    rng = random.Random(100 + d)
+    for _ in range(60):
+        sigma = rng.choice([2, 4, 20])
+        alpha = "ACGTNRDQEHIKLMFPSWYV"[:sigma]
+        l = rng.randint(1, 7)
+        e = rng.randint(0, l - 1)
+        p = "".join(rng.choice(alpha) for _ in range(rng.randint(l, 18)))
+        t = "".join(rng.choice(alpha) for _ in range(rng.randint(1, 22)))
+        assert port_pair(d, l, e, p, t) == brute_pair(d, l, e, p, t), (d, l, e, p, t)

@@ -172,6 +172,32 @@ uint64_t motex_ctx_launches ( const motex_ctx * ctx );
  */
 int motex_probe_int_peak ( int device, double * lop3_tops, double * iadd_tops, double * popc_tops );
 
+/*
+ * Per-pair factor search that allocates nothing (no counterpart in the
+ * reference).  For callers that cannot call cudaMalloc -- code inside another
+ * framework's memory pool or allocator hooks, code holding a fixed memory
+ * budget, plug-ins that are only handed device buffers.  Same result as
+ * motex_gpu_extract_pair for plain motifs: for every factor of p ending at
+ * j, d_u[j] += 1 if it occurs in t, d_v[j] += its occurrences.  Differences:
+ *   - d_p (m bytes), d_t (n bytes), d_u and d_v (m entries each) are DEVICE
+ *     pointers owned by the caller; work is queued on `stream` (a
+ *     cudaStream_t; 0 = default stream) of the current device, and the call
+ *     returns after that stream has finished it;
+ *   - symbols are coded by their index in `alphabet` (e.g. "ACGTN"; at most
+ *     32 symbols); a byte outside it makes the call return MOTEX_EINVAL and
+ *     leaves d_u / d_v untouched;
+ *   - limits: l <= 32, m <= 32768, n <= 1048576, no structured motifs;
+ *     larger sizes return MOTEX_EUNSUPPORTED.
+ * All intermediate data lives in one 4 MiB static device array that every
+ * GPU loading this library keeps until the process exits.  The first call
+ * on a device resolves that array's address (with the device current), so
+ * make it before any stream capture.  Calls share the array: calls that
+ * overlap on the GPU race and must be serialised by the caller.
+ */
+int motex_gpu_extract_pair_static ( const motex_params * prm, const char * alphabet,
+                                    const char * d_p, uint32_t m, const char * d_t, uint32_t n,
+                                    uint32_t * d_u, uint32_t * d_v, void * stream );
+
 #ifdef __cplusplus
 }
 #endif

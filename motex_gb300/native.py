@@ -23,6 +23,7 @@ EXPORTS = [
     "motex_ctx_create", "motex_ctx_destroy", "motex_gpu_run", "motex_result_free",
     "motex_gpu_load", "motex_gpu_execute", "motex_gpu_fetch", "motex_gpu_extract_pair",
     "motex_gpu_strerror", "motex_gpu_last_error", "motex_ctx_launches", "motex_probe_int_peak",
+    "motex_gpu_extract_pair_static",
 ]
 
 
@@ -76,6 +77,8 @@ def load_library(path: str = LIB_PATH):
         "motex_gpu_last_error": (C.c_char_p, []),
         "motex_ctx_launches": (C.c_uint64, [C.c_void_p]),
         "motex_probe_int_peak": (C.c_int, [C.c_int, P(C.c_double), P(C.c_double), P(C.c_double)]),
+        "motex_gpu_extract_pair_static": (C.c_int, [P(Params), C.c_char_p, C.c_void_p, C.c_uint32, C.c_void_p,
+                                                    C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)

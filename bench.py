@@ -41,11 +41,11 @@ sys.path.insert(0, ROOT)
 from motex_gb300 import workloads as W  # noqa: E402
 
 WORKLOADS = {
-    "dna_ed": lambda: W.dna_ed(),
-    "dna_hd_small": lambda: W.dna_hd_small(),
-    "prot_uneven_d0": lambda: W.prot_uneven(d=0),
-    "prot_uneven_d1": lambda: W.prot_uneven(d=1),
-    "dna_long": lambda: W.dna_long(),
+    "dna_ed": lambda s: W.dna_ed(scale=s),
+    "dna_hd_small": lambda s: W.dna_hd_small(scale=s),
+    "prot_uneven_d0": lambda s: W.prot_uneven(d=0, scale=s),
+    "prot_uneven_d1": lambda s: W.prot_uneven(d=1, scale=s),
+    "dna_long": lambda s: W.dna_long(scale=s),
 }
 DEFAULT_WORKLOAD = "dna_ed"
 # algorithmic integer operations per DP cell (one factor x one text position)
@@ -196,7 +196,7 @@ def run_gpu(args, rank, world, local_rank):
     from motex_gb300 import native
 
     torch.cuda.set_device(local_rank)
-    wl = WORKLOADS[args.workload]()
+    wl = WORKLOADS[args.workload](args.scale)
     prm = native.make_params(wl.d, wl.k, wl.e, wl.q, wl.Q, wl.n, wl.N, wl.boxes)
     ctx = native.Context(local_rank)
     lib = ctx.lib
@@ -290,7 +290,7 @@ def run_gpu(args, rank, world, local_rank):
         "value": round(value, 2), "unit": "GCUPS", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": round(step_s * 1e3 / args.steps, 3), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "u32 bit-vector (integer)", "data": "synthetic (seeded generator)",
-        "config": {"workload": args.workload, "alphabet": wl.alphabet, "num_seqs": len(wl.seqs),
+        "config": {"workload": args.workload, "scale": args.scale, "alphabet": wl.alphabet, "num_seqs": len(wl.seqs),
                    "total_len": total_pos, "d": wl.d, "k": wl.k, "e": wl.e, "q": wl.q,
                    "ref_cells": cells, "unique_words": first.unique_words, "motifs": len(first.motifs),
                    "parallelism": f"replicas{world}", "l2": "flushed (256 MiB write) before every step",
@@ -308,7 +308,7 @@ def run_gpu(args, rank, world, local_rank):
 
 def run_reference(args):
     """Reference arm: the CPU implementation of the path, all host threads."""
-    wl = WORKLOADS[args.workload]()
+    wl = WORKLOADS[args.workload](args.scale)
     binary, kind = cpu_binary()
     threads = os.cpu_count() or 1
     sample = cpu_sample(binary, wl, threads, target_s=8.0)
@@ -339,6 +339,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS))
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--scale", type=float, default=1.0,
+                    help="shrink the workload (profiling captures only; 1.0 = the benchmark size)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup

@@ -22,6 +22,8 @@
 // it once however many chunks saw it.
 #include "kernels.cuh"
 
+#include <algorithm>
+
 namespace mtx
 {
 
@@ -71,7 +73,7 @@ __device__ __forceinline__ void finish_chunk ( const DPArgs & a, const ChunkInfo
 
 } // namespace
 
-template <int B, int W, bool ED, bool SCALED>
+template <int B, int W, bool ED, bool SCALED, int UR>
 __global__ void __launch_bounds__ ( kDPThreads ) k_dp_fast ( const DPArgs a )
 {
     const uint32_t base = blockIdx.x * ( kDPThreads * W ) + threadIdx.x;
@@ -106,20 +108,24 @@ __global__ void __launch_bounds__ ( kDPThreads ) k_dp_fast ( const DPArgs a )
             const uint32_t vm = __ldg ( a.text.vmask + k ), em = __ldg ( a.text.emask + k );
             if ( vm == 0xffffffffu && em == 0u )
             {
-#pragma unroll
-                for ( int r = 0; r < 32; ++r )
+#pragma unroll 1
+                for ( int g = 0; g < 32; g += UR )
                 {
-                    uint32_t y[B];
 #pragma unroll
-                    for ( int b = 0; b < B; ++b )
-                        y[b] = ( r == 31 ? cur[b] : __funnelshift_r ( prev[b], cur[b], r + 1 ) ) & topmask;
-#pragma unroll
-                    for ( int i = 0; i < W; ++i )
+                    for ( int rr = 0; rr < UR; ++rr )
                     {
-                        uint32_t x = wp[i][0] ^ y[0];
+                        const int r = g + rr;
+                        uint32_t y[B];
 #pragma unroll
-                        for ( int b = 1; b < B; ++b ) x |= wp[i][b] ^ y[b];
-                        cnt[i] += __popc ( x ) <= e;
+                        for ( int b = 0; b < B; ++b ) y[b] = __funnelshift_rc ( prev[b], cur[b], r + 1 ) & topmask;
+#pragma unroll
+                        for ( int i = 0; i < W; ++i )
+                        {
+                            uint32_t x = wp[i][0] ^ y[0];
+#pragma unroll
+                            for ( int b = 1; b < B; ++b ) x |= wp[i][b] ^ y[b];
+                            cnt[i] += __popc ( x ) <= e;
+                        }
                     }
                 }
             }
@@ -190,17 +196,24 @@ __global__ void __launch_bounds__ ( kDPThreads ) k_dp_fast ( const DPArgs a )
             const bool counting = k >= ch.begin;
             if ( counting && vm == 0xffffffffu && em == 0u )
             {
-#pragma unroll
-                for ( int r = 0; r < 32; ++r )
+#pragma unroll 1
+                for ( int g = 0; g < 32; g += UR )
                 {
-                    uint32_t T[B];
+                    uint32_t cg[B];
 #pragma unroll
-                    for ( int b = 0; b < B; ++b ) T[b] = 0u - ( ( cur[b] >> r ) & 1u );
+                    for ( int b = 0; b < B; ++b ) cg[b] = cur[b] >> g;
 #pragma unroll
-                    for ( int i = 0; i < W; ++i )
+                    for ( int rr = 0; rr < UR; ++rr )
                     {
-                        step ( i, T );
-                        cnt[i] += sc[i] < thr;
+                        uint32_t T[B];
+#pragma unroll
+                        for ( int b = 0; b < B; ++b ) T[b] = 0u - ( ( cg[b] >> rr ) & 1u );
+#pragma unroll
+                        for ( int i = 0; i < W; ++i )
+                        {
+                            step ( i, T );
+                            cnt[i] += sc[i] < thr;
+                        }
                     }
                 }
             }
@@ -356,41 +369,303 @@ __global__ void __launch_bounds__ ( kDPThreads ) k_dp_generic ( const DPArgs a, 
     finish_chunk<1> ( a, ch, base, cnt, uacc, vacc );
 }
 
-// ------------------------------------------------------------------ launchers
-
-template <int B, int W>
-static bool launch_fast_bw ( const DPArgs & a, bool ed, dim3 grid, cudaStream_t st )
+/*
+ * Edit distance with NL factors per 32-bit register (SWAR), l <= 15.
+ * Lane i holds a factor in bits [i*S, i*S+l), S = l+1, with a guard bit at
+ * i*S+l.  The text bits are cleared at the guards, so Eq has 1 there; Pv and
+ * Mv keep 0 there (Mv through the NG mask, Pv because the Mh that is shifted
+ * up is taken without the lanes' top bits).  With those invariants no carry
+ * of (Eq&Pv)+Pv and no shifted Ph/Mh bit crosses into the next lane.  The
+ * per-lane scores live in bit fields at i*S (each in [0, l]); the hit test
+ * adds 2^(l-1)-(e+1) per field and reads bit l-1 of each field.  Hits are
+ * counted in per-lane fields and moved to shared memory every 32 positions.
+ */
+struct SwarConst
 {
-    if ( ! ed )
-        k_dp_fast<B, W, false, false><<<grid, kDPThreads, 0, st>>> ( a );
-    else if ( a.l <= 28 )
-        k_dp_fast<B, W, true, true><<<grid, kDPThreads, 0, st>>> ( a );
-    else
-        k_dp_fast<B, W, true, false><<<grid, kDPThreads, 0, st>>> ( a );
-    return true;
+    uint32_t HB;     // bit l-1 of every lane
+    uint32_t NG;     // all bits but the guards
+    uint32_t NGm1;   // NG without the lanes' top bits
+    uint32_t K;      // per field 2^(l-1) - (e+1)
+    uint32_t SC0;    // per field score l
+    uint32_t S;      // lane stride
+    uint32_t FM;     // field mask (S bits)
+};
+
+template <int B, int NL, int W, int UR>
+__global__ void __launch_bounds__ ( kDPThreads ) k_dp_swar_ed ( const DPArgs a, const SwarConst C )
+{
+    extern __shared__ uint32_t smem[];
+    constexpr int NF = W * NL;                      // factors per thread
+    // [field][thread]: count in the current text, texts seen, occurrences
+    uint32_t * s_cnt = smem;
+    uint32_t * s_u = smem + NF * kDPThreads;
+    uint32_t * s_v = smem + 2 * NF * kDPThreads;
+    const int tid = threadIdx.x;
+    for ( int f = 0; f < NF; ++f ) s_cnt[f * kDPThreads + tid] = s_u[f * kDPThreads + tid] = s_v[f * kDPThreads + tid] = 0;
+
+    const uint32_t gbase = blockIdx.x * ( kDPThreads * W ) + tid;       // first factor group of this thread
+    const uint32_t l = a.l, sh = l - 1;
+    uint32_t wp[W][B];
+#pragma unroll
+    for ( int i = 0; i < W; ++i )
+    {
+#pragma unroll
+        for ( int b = 0; b < B; ++b ) wp[i][b] = 0;
+        const uint32_t g = gbase + i * kDPThreads;
+#pragma unroll
+        for ( int j = 0; j < NL; ++j )
+        {
+            const uint32_t w = g * NL + j;
+            if ( w < a.U )
+#pragma unroll
+                for ( int b = 0; b < B; ++b ) wp[i][b] |= __ldg ( a.wplanes32 + ( size_t ) b * a.U + w ) << ( j * C.S );
+        }
+    }
+    uint32_t Pv[W], Mv[W], sc[W], cnt[W];
+#pragma unroll
+    for ( int i = 0; i < W; ++i ) { Pv[i] = C.NG; Mv[i] = 0; sc[i] = C.SC0; cnt[i] = 0; }
+
+    const ChunkInfo ch = a.chunks[blockIdx.y];
+    int cur_split = ch.first_split;
+    const uint32_t * __restrict__ planes = a.text.planes;
+    const uint32_t stride = a.text.plane_stride;
+
+    auto step = [&] ( int i, const uint32_t ( &T )[B] ) {
+        uint32_t x = wp[i][0] ^ T[0];
+#pragma unroll
+        for ( int b = 1; b < B; ++b ) x |= wp[i][b] ^ T[b];
+        const uint32_t Xv = ~x | Mv[i];
+        const uint32_t s = ( ~x & Pv[i] ) + Pv[i];
+        const uint32_t Xh = ( s ^ Pv[i] ) | ~x;
+        const uint32_t Ph = Mv[i] | ~( Xh | Pv[i] );
+        const uint32_t Mhs = Pv[i] & Xh & C.NGm1;
+        const uint32_t mh = Pv[i] & Xh & C.HB;
+        const uint32_t ph = Ph & C.HB;
+        sc[i] = sc[i] + ( ph >> sh ) - ( mh >> sh );
+        const uint32_t Ph2 = Ph << 1, Mh2 = Mhs << 1;
+        Pv[i] = Mh2 | ~( Xv | Ph2 );
+        Mv[i] = Ph2 & Xv & C.NG;
+    };
+    auto count = [&] ( int i ) { cnt[i] += ( ~( sc[i] + C.K ) & C.HB ) >> sh; };
+    auto drain = [&] () {                           // register fields -> shared counters
+#pragma unroll
+        for ( int i = 0; i < W; ++i )
+        {
+#pragma unroll
+            for ( int j = 0; j < NL; ++j ) s_cnt[( i * NL + j ) * kDPThreads + tid] += ( cnt[i] >> ( j * C.S ) ) & C.FM;
+            cnt[i] = 0;
+        }
+    };
+    auto end_sequence = [&] () {
+        for ( int f = 0; f < NF; ++f )
+        {
+            const uint32_t c = s_cnt[f * kDPThreads + tid];
+            if ( ! c ) continue;
+            if ( cur_split < 0 ) s_u[f * kDPThreads + tid] += 1;
+            else
+            {
+                const uint32_t w = ( gbase + ( f / NL ) * kDPThreads ) * NL + ( f % NL );
+                if ( w < a.U ) a.split_flags[( size_t ) cur_split * a.U + w] = 1;
+            }
+            s_v[f * kDPThreads + tid] += c;
+            s_cnt[f * kDPThreads + tid] = 0;
+        }
+    };
+
+    for ( uint32_t k = ch.warm; k < ch.end; ++k )
+    {
+        uint32_t cur[B];
+#pragma unroll
+        for ( int b = 0; b < B; ++b ) cur[b] = __ldg ( planes + ( size_t ) b * stride + k + 1 );
+        const uint32_t vm = __ldg ( a.text.vmask + k ), em = __ldg ( a.text.emask + k );
+        const bool counting = k >= ch.begin;
+        if ( counting && vm == 0xffffffffu && em == 0u )
+        {
+#pragma unroll 1
+            for ( int g = 0; g < 32; g += UR )
+            {
+                uint32_t cg[B];
+#pragma unroll
+                for ( int b = 0; b < B; ++b ) cg[b] = cur[b] >> g;
+#pragma unroll
+                for ( int rr = 0; rr < UR; ++rr )
+                {
+                    uint32_t T[B];
+#pragma unroll
+                    for ( int b = 0; b < B; ++b ) T[b] = ( 0u - ( ( cg[b] >> rr ) & 1u ) ) & C.NG;
+#pragma unroll
+                    for ( int i = 0; i < W; ++i )
+                    {
+                        step ( i, T );
+                        count ( i );
+                    }
+                }
+            }
+        }
+        else
+        {
+            for ( int r = 0; r < 32; ++r )
+            {
+                uint32_t T[B];
+#pragma unroll
+                for ( int b = 0; b < B; ++b ) T[b] = ( 0u - ( ( cur[b] >> r ) & 1u ) ) & C.NG;
+                const bool count_here = counting && ( ( vm >> r ) & 1u );
+#pragma unroll
+                for ( int i = 0; i < W; ++i )
+                {
+                    step ( i, T );
+                    if ( count_here ) count ( i );
+                }
+                if ( ( em >> r ) & 1u )
+                {
+                    if ( counting )
+                    {
+                        drain ();
+                        end_sequence ();
+                        cur_split = -1;
+                    }
+#pragma unroll
+                    for ( int i = 0; i < W; ++i ) { Pv[i] = C.NG; Mv[i] = 0; sc[i] = C.SC0; }
+                }
+            }
+        }
+        drain ();
+    }
+    // chunk end
+    for ( int f = 0; f < NF; ++f )
+    {
+        const uint32_t w = ( gbase + ( f / NL ) * kDPThreads ) * NL + ( f % NL );
+        if ( w >= a.U ) continue;
+        const uint32_t c = s_cnt[f * kDPThreads + tid];
+        uint32_t u = s_u[f * kDPThreads + tid];
+        if ( c )
+        {
+            if ( ch.last_split >= 0 ) a.split_flags[( size_t ) ch.last_split * a.U + w] = 1;
+            else u += 1;
+        }
+        const uint32_t v = s_v[f * kDPThreads + tid] + c;
+        if ( u ) atomicAdd ( a.u_acc + w, u );
+        if ( v ) atomicAdd ( a.v_acc + w, v );
+    }
 }
 
-template <int B>
-static bool launch_fast_b ( const DPArgs & a, int W, bool ed, dim3 grid, cudaStream_t st )
+// ------------------------------------------------------------------ launchers
+
+template <int B, int W, int UR>
+static void launch_fast_bwu ( const DPArgs & a, bool ed, dim3 grid, cudaStream_t st )
 {
-    switch ( W )
+    if ( ! ed )
+        k_dp_fast<B, W, false, false, UR><<<grid, kDPThreads, 0, st>>> ( a );
+    else if ( a.l <= 28 )
+        k_dp_fast<B, W, true, true, UR><<<grid, kDPThreads, 0, st>>> ( a );
+    else
+        k_dp_fast<B, W, true, false, UR><<<grid, kDPThreads, 0, st>>> ( a );
+}
+
+template <int B, int W>
+static bool launch_fast_bw ( const DPArgs & a, int UR, bool ed, dim3 grid, cudaStream_t st )
+{
+    switch ( UR )
     {
-        case 4: return launch_fast_bw<B, 4> ( a, ed, grid, st );
-        case 8: return launch_fast_bw<B, 8> ( a, ed, grid, st );
+        case 4: launch_fast_bwu<B, W, 4> ( a, ed, grid, st ); return true;
+        case 8: launch_fast_bwu<B, W, 8> ( a, ed, grid, st ); return true;
+        case 32: launch_fast_bwu<B, W, 32> ( a, ed, grid, st ); return true;
         default: return false;
     }
 }
 
-bool launch_dp_fast ( const DPArgs & a, int B, int W, bool ed, dim3 grid, cudaStream_t st )
+template <int B>
+static bool launch_fast_b ( const DPArgs & a, int W, int UR, bool ed, dim3 grid, cudaStream_t st )
+{
+    switch ( W )
+    {
+        case 4: return launch_fast_bw<B, 4> ( a, UR, ed, grid, st );
+        case 8: return launch_fast_bw<B, 8> ( a, UR, ed, grid, st );
+        default: return false;
+    }
+}
+
+bool launch_dp_fast ( const DPArgs & a, int B, int W, int UR, bool ed, dim3 grid, cudaStream_t st )
 {
     if ( a.l < 1 || a.l > 32 ) return false;
     switch ( B )
     {
-        case 1: return launch_fast_b<1> ( a, W, ed, grid, st );
-        case 2: return launch_fast_b<2> ( a, W, ed, grid, st );
-        case 3: return launch_fast_b<3> ( a, W, ed, grid, st );
-        case 4: return launch_fast_b<4> ( a, W, ed, grid, st );
-        case 5: return launch_fast_b<5> ( a, W, ed, grid, st );
+        case 1:                                     // runs on the 2-plane kernel (plane 1 is zero)
+        case 2: return launch_fast_b<2> ( a, W, UR, ed, grid, st );
+        case 3: return launch_fast_b<3> ( a, W, UR, ed, grid, st );
+        case 4: return launch_fast_b<4> ( a, W, UR, ed, grid, st );
+        case 5: return launch_fast_b<5> ( a, W, UR, ed, grid, st );
+        default: return false;
+    }
+}
+
+int swar_lanes ( uint32_t l )
+{
+    if ( l < 4 || l > 15 ) return 1;
+    return std::min ( 4, 33 / ( int ) ( l + 1 ) );
+}
+
+template <int B, int NL, int W>
+static bool launch_swar_bnw ( const DPArgs & a, const SwarConst & C, int UR, dim3 grid, cudaStream_t st )
+{
+    const size_t smem = ( size_t ) 3 * W * NL * kDPThreads * sizeof ( uint32_t );
+    switch ( UR )
+    {
+        case 4: k_dp_swar_ed<B, NL, W, 4><<<grid, kDPThreads, smem, st>>> ( a, C ); return true;
+        case 8: k_dp_swar_ed<B, NL, W, 8><<<grid, kDPThreads, smem, st>>> ( a, C ); return true;
+        default: return false;
+    }
+}
+
+template <int B, int NL>
+static bool launch_swar_bn ( const DPArgs & a, const SwarConst & C, int W, int UR, dim3 grid, cudaStream_t st )
+{
+    switch ( W )
+    {
+        case 4: return launch_swar_bnw<B, NL, 4> ( a, C, UR, grid, st );
+        case 8: return launch_swar_bnw<B, NL, 8> ( a, C, UR, grid, st );
+        default: return false;
+    }
+}
+
+template <int B>
+static bool launch_swar_b ( const DPArgs & a, const SwarConst & C, int NL, int W, int UR, dim3 grid, cudaStream_t st )
+{
+    switch ( NL )
+    {
+        case 2: return launch_swar_bn<B, 2> ( a, C, W, UR, grid, st );
+        case 3: return launch_swar_bn<B, 3> ( a, C, W, UR, grid, st );
+        case 4: return launch_swar_bn<B, 4> ( a, C, W, UR, grid, st );
+        default: return false;
+    }
+}
+
+bool launch_dp_swar_ed ( const DPArgs & a, int B, int NL, int W, int UR, dim3 grid, cudaStream_t st )
+{
+    const uint32_t l = a.l;
+    if ( NL < 2 || NL != swar_lanes ( l ) ) return false;
+    SwarConst C;
+    C.S = l + 1;
+    C.HB = C.NG = C.K = C.SC0 = 0;
+    uint32_t guards = 0;
+    for ( int j = 0; j < NL; ++j )
+    {
+        const uint32_t o = j * C.S;
+        C.HB |= 1u << ( o + l - 1 );
+        if ( o + l < 32 ) guards |= 1u << ( o + l );
+        C.K += ( ( 1u << ( l - 1 ) ) - ( a.e + 1 ) ) << o;
+        C.SC0 += l << o;
+    }
+    C.NG = ~guards;
+    C.NGm1 = C.NG & ~C.HB;
+    C.FM = ( 1u << C.S ) - 1u;
+    switch ( B )
+    {
+        case 1:
+        case 2: return launch_swar_b<2> ( a, C, NL, W, UR, grid, st );
+        case 3: return launch_swar_b<3> ( a, C, NL, W, UR, grid, st );
+        case 4: return launch_swar_b<4> ( a, C, NL, W, UR, grid, st );
+        case 5: return launch_swar_b<5> ( a, C, NL, W, UR, grid, st );
         default: return false;
     }
 }

@@ -1,0 +1,284 @@
+// Structured-motif search (two boxes, one gap) of the GB300 engine.
+//
+// Reference semantics (functions.cc:564-705 Hamming, 773-915 edit distance):
+// for pattern position jx (end of box 0 in sequence x) and gap choice k of
+// x, and every text position it (end of box 0 in text t) and gap choice l
+// of t, the pair counts when box 0 matches at (it, jx) with <= e errors and
+// box 1 -- x[jx+S_k+1 .. jx+S_k+b1] -- matches the text box ending at
+// p = it+S_l+b1 with <= e1 errors, p inside t.  v[k, jx] counts the (it, l)
+// combinations over all texts, u[k, jx] the texts with at least one.
+//
+// A warp owns 32 consecutive pattern positions P0..P0+31 (box-0 rows, one per
+// lane) and the 32+G-1 box-1 rows P0+gmin+b1 .. P0+31+gmax+b1 they need
+// (G = gmax-gmin+1 gap choices; lane r runs rows r and r+32).  All lanes walk
+// the same text positions.  Box-1 hits are exchanged by two ballots; each
+// lane keeps a shift register of its box-0 hits (bit d = hit at p-d), so a
+// box-1 hit of row P0+lane+gmin+b1+k at p adds popc(history & bits
+// [gmin+b1, gmax+b1]) to v[k, P0+lane] -- all text gap choices at once.
+#include "kernels.cuh"
+
+namespace mtx
+{
+
+namespace
+{
+
+// Edit-distance column step (Myers/Hyyro, l <= 32); returns the new score.
+template <int B>
+__device__ __forceinline__ uint32_t ed_step ( const uint32_t ( &w )[B], const uint32_t ( &T )[B], uint32_t & Pv,
+                                              uint32_t & Mv, uint32_t sc, uint32_t sh )
+{
+    uint32_t x = w[0] ^ T[0];
+#pragma unroll
+    for ( int b = 1; b < B; ++b ) x |= w[b] ^ T[b];
+    const uint32_t Eq = ~x;
+    const uint32_t Xv = Eq | Mv;
+    const uint32_t Xh = ( ( ( Eq & Pv ) + Pv ) ^ Pv ) | Eq;
+    uint32_t Ph = Mv | ~( Xh | Pv );
+    uint32_t Mh = Pv & Xh;
+    sc += ( ( Ph >> sh ) & 1u ) - ( ( Mh >> sh ) & 1u );
+    Ph <<= 1;
+    Mh <<= 1;
+    Pv = Mh | ~( Xv | Ph );
+    Mv = Ph & Xv;
+    return sc;
+}
+
+template <int B>
+__device__ __forceinline__ bool hd_hit ( const uint32_t ( &w )[B], const uint32_t ( &Y )[B], uint32_t mask, uint32_t e )
+{
+    uint32_t x = ( w[0] ^ Y[0] );
+#pragma unroll
+    for ( int b = 1; b < B; ++b ) x |= w[b] ^ Y[b];
+    return __popc ( x & mask ) <= e;
+}
+
+} // namespace
+
+template <int B, bool ED>
+__global__ void __launch_bounds__ ( kDPThreads ) k_dp_struct1 ( const StructArgs a )
+{
+    extern __shared__ uint32_t smem[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t G = a.G;
+    // per (thread, k): hit count in the current text, texts seen, occurrences
+    uint32_t * s_cnt = smem + ( size_t ) threadIdx.x * G * 3;
+    uint32_t * s_u = s_cnt + G;
+    uint32_t * s_v = s_u + G;
+    for ( uint32_t k = 0; k < G; ++k ) s_cnt[k] = s_u[k] = s_v[k] = 0;
+
+    const uint32_t P0 = ( blockIdx.x * ( kDPThreads / 32 ) + warp ) * 32;
+    const uint32_t jx = P0 + lane;
+    const uint32_t r0 = P0 + a.gmin + a.b1 + lane;               // box-1 rows of this lane
+    const uint32_t r1 = r0 + 32;
+    const bool has_r1 = lane + 1 < ( int ) G;
+
+    uint32_t w0[B], w1a[B], w1b[B];
+#pragma unroll
+    for ( int b = 0; b < B; ++b )
+    {
+        w0[b] = jx < a.total ? a.wpl0[( size_t ) b * a.total + jx] : 0u;
+        w1a[b] = r0 < a.total ? a.wpl1[( size_t ) b * a.total + r0] : 0u;
+        w1b[b] = ( has_r1 && r1 < a.total ) ? a.wpl1[( size_t ) b * a.total + r1] : 0u;
+    }
+    // gap choices k of x whose box 1 stays inside x's sequence
+    uint32_t kvalid = 0;
+    if ( jx < a.total && a.row_ok[jx] )
+    {
+        const uint32_t xend = a.row_end[jx];
+        for ( uint32_t k = 0; k < G; ++k )
+            if ( jx + a.gmin + k + a.b1 < xend ) kvalid |= 1u << k;
+    }
+    const uint32_t Gmask = G >= 32 ? 0xffffffffu : ( ( 1u << G ) - 1u );
+    const uint32_t win = ( ( a.gmax + a.b1 >= 31 ) ? 0xffffffffu : ( ( 2u << ( a.gmax + a.b1 ) ) - 1u ) ) &
+                         ~( ( 1u << ( a.gmin + a.b1 ) ) - 1u );
+
+    const ChunkInfo ch = a.chunks[blockIdx.y];
+    int cur_split = ch.first_split;
+    const uint32_t * __restrict__ planes = a.text.planes;
+    const uint32_t stride = a.text.plane_stride;
+    const uint32_t l0 = a.l0, l1 = a.l1;
+    const uint32_t top0 = l0 >= 32 ? 0xffffffffu : ~( ( 1u << ( 32 - l0 ) ) - 1u );
+    const uint32_t top1 = l1 >= 32 ? 0xffffffffu : ~( ( 1u << ( 32 - l1 ) ) - 1u );
+    uint32_t hist = 0;
+    uint32_t Pv0 = ~0u, Mv0 = 0, sc0 = l0, Pva = ~0u, Mva = 0, sca = l1, Pvb = ~0u, Mvb = 0, scb = l1;
+
+    auto flush = [&] () {
+        for ( uint32_t k = 0; k < G; ++k )
+        {
+            const uint32_t c = s_cnt[k];
+            if ( ! c ) continue;
+            if ( cur_split < 0 ) s_u[k] += 1;
+            else if ( jx < a.total ) a.split_flags[( ( size_t ) cur_split * a.total + jx ) * G + k] = 1;
+            s_v[k] += c;
+            s_cnt[k] = 0;
+        }
+    };
+
+    uint32_t prev[B];
+#pragma unroll
+    for ( int b = 0; b < B; ++b ) prev[b] = __ldg ( planes + ( size_t ) b * stride + ch.warm );
+    for ( uint32_t kb = ch.warm; kb < ch.end; ++kb )
+    {
+        uint32_t cur[B];
+#pragma unroll
+        for ( int b = 0; b < B; ++b ) cur[b] = __ldg ( planes + ( size_t ) b * stride + kb + 1 );
+        const uint32_t vm = __ldg ( a.text.vmask + kb ), em = __ldg ( a.text.emask + kb );
+        const bool counting = kb >= ch.begin;
+        for ( int r = 0; r < 32; ++r )
+        {
+            bool h0, ha, hb = false;
+            if constexpr ( ED )
+            {
+                uint32_t T[B];
+#pragma unroll
+                for ( int b = 0; b < B; ++b ) T[b] = 0u - ( ( cur[b] >> r ) & 1u );
+                sc0 = ed_step<B> ( w0, T, Pv0, Mv0, sc0, l0 - 1 );
+                sca = ed_step<B> ( w1a, T, Pva, Mva, sca, l1 - 1 );
+                if ( has_r1 ) scb = ed_step<B> ( w1b, T, Pvb, Mvb, scb, l1 - 1 );
+                h0 = sc0 <= a.e0;
+                ha = sca <= a.e1;
+                hb = has_r1 && scb <= a.e1;
+            }
+            else
+            {
+                uint32_t Y[B];
+#pragma unroll
+                for ( int b = 0; b < B; ++b ) Y[b] = __funnelshift_rc ( prev[b], cur[b], r + 1 );
+                h0 = hd_hit<B> ( w0, Y, top0, a.e0 );
+                ha = hd_hit<B> ( w1a, Y, top1, a.e1 );
+                hb = has_r1 && hd_hit<B> ( w1b, Y, top1, a.e1 );
+            }
+            h0 = h0 && ( ( vm >> r ) & 1u );           // box 0 must end a valid match
+            hist = ( hist << 1 ) | ( uint32_t ) h0;
+            const uint32_t Ha = __ballot_sync ( 0xffffffffu, ha ), Hb = __ballot_sync ( 0xffffffffu, hb );
+            if ( counting && ( Ha | Hb ) )
+            {
+                const uint64_t H = ( ( uint64_t ) Hb << 32 ) | Ha;
+                const uint32_t g = ( uint32_t ) ( H >> lane ) & Gmask & kvalid;
+                if ( g )
+                {
+                    const uint32_t c = __popc ( hist & win );
+                    if ( c )
+                        for ( uint32_t k = 0; k < G; ++k )
+                            if ( ( g >> k ) & 1u ) s_cnt[k] += c;
+                }
+            }
+            if ( ( em >> r ) & 1u )
+            {
+                if ( counting )
+                {
+                    flush ();
+                    cur_split = -1;
+                }
+                hist = 0;
+                Pv0 = Pva = Pvb = ~0u;
+                Mv0 = Mva = Mvb = 0;
+                sc0 = l0;
+                sca = scb = l1;
+            }
+        }
+#pragma unroll
+        for ( int b = 0; b < B; ++b ) prev[b] = cur[b];
+    }
+    // chunk end: the text cut by the boundary records presence in its split row
+    for ( uint32_t k = 0; k < G; ++k )
+    {
+        const uint32_t c = s_cnt[k];
+        if ( c )
+        {
+            if ( ch.last_split >= 0 && jx < a.total )
+                a.split_flags[( ( size_t ) ch.last_split * a.total + jx ) * G + k] = 1;
+            else
+                s_u[k] += 1;
+            s_v[k] += c;
+        }
+        if ( jx < a.total && ( s_u[k] | s_v[k] ) )
+        {
+            atomicAdd ( a.u_acc + ( size_t ) jx * G + k, s_u[k] );
+            atomicAdd ( a.v_acc + ( size_t ) jx * G + k, s_v[k] );
+        }
+    }
+}
+
+template <int B>
+static void launch_struct_b ( const StructArgs & a, bool ed, dim3 grid, size_t smem, cudaStream_t st )
+{
+    if ( ed ) k_dp_struct1<B, true><<<grid, kDPThreads, smem, st>>> ( a );
+    else k_dp_struct1<B, false><<<grid, kDPThreads, smem, st>>> ( a );
+}
+
+bool launch_dp_struct1 ( const StructArgs & a, int B, bool ed, dim3 grid, cudaStream_t st )
+{
+    if ( a.l0 < 1 || a.l0 > 32 || a.l1 < 1 || a.l1 > 32 || a.G < 1 || a.G > 32 ) return false;
+    if ( a.gmax + a.b1 > 31 ) return false;
+    const size_t smem = ( size_t ) kDPThreads * a.G * 3 * sizeof ( uint32_t );
+    if ( smem > 48 * 1024 ) return false;
+    switch ( B )
+    {
+        case 1: launch_struct_b<1> ( a, ed, grid, smem, st ); return true;
+        case 2: launch_struct_b<2> ( a, ed, grid, smem, st ); return true;
+        case 3: launch_struct_b<3> ( a, ed, grid, smem, st ); return true;
+        case 4: launch_struct_b<4> ( a, ed, grid, smem, st ); return true;
+        case 5: launch_struct_b<5> ( a, ed, grid, smem, st ); return true;
+        default: return false;
+    }
+}
+
+// Bit planes of the factor of length l ending at every position (zero where
+// it would start before position 0); top-aligned for Hamming.
+__global__ void k_wplanes_all ( const uint8_t * __restrict__ codes, uint32_t total, uint32_t l, uint32_t B,
+                                int top_aligned, uint32_t * __restrict__ out )
+{
+    const uint32_t pos = blockIdx.x * blockDim.x + threadIdx.x;
+    if ( pos >= total ) return;
+    uint32_t pl[kMaxPlanes] = { 0, 0, 0, 0, 0 };
+    if ( pos + 1 >= l )
+        for ( uint32_t q = 0; q < l; ++q )
+        {
+            const uint32_t c = codes[pos + 1 - l + q];
+            const uint32_t bit = top_aligned ? ( 32 - l + q ) : q;
+#pragma unroll
+            for ( int b = 0; b < kMaxPlanes; ++b ) pl[b] |= ( ( c >> b ) & 1u ) << bit;
+        }
+    for ( uint32_t b = 0; b < B; ++b ) out[( size_t ) b * total + pos] = pl[b];
+}
+
+// Row bookkeeping of the pattern side: row_ok = box 0 may end here (sequence
+// long enough, full box inside it), row_end = end offset of its sequence.
+__global__ void k_struct_rows ( const uint32_t * __restrict__ offs, uint32_t nseq, uint64_t total, uint32_t l0,
+                                uint32_t tml, int pair_mode, uint8_t * row_ok, uint32_t * row_end )
+{
+    const uint32_t pos = blockIdx.x * blockDim.x + threadIdx.x;
+    if ( pos >= total ) return;
+    uint32_t lo = 0, hi = nseq;
+    while ( hi - lo > 1 )
+    {
+        const uint32_t mid = ( lo + hi ) >> 1;
+        if ( offs[mid] <= pos ) lo = mid; else hi = mid;
+    }
+    while ( offs[lo + 1] <= pos ) ++lo;
+    const uint32_t start = offs[lo], end = offs[lo + 1];
+    row_end[pos] = end;
+    row_ok[pos] = ( end - start ) >= tml && pos - start + 1 >= l0 && ( ! pair_mode || lo == 0 );
+}
+
+/*
+ * Per (position, gap choice): add split-row presence, apply the quorum
+ * filter and mark passing entries (pattern side of whole-set runs), or copy
+ * totals out (pair mode).
+ */
+__global__ void k_struct_finalize ( StructFinalizeArgs a )
+{
+    const uint64_t i = ( uint64_t ) blockIdx.x * blockDim.x + threadIdx.x;
+    if ( i >= a.n ) return;
+    uint32_t u = a.u_acc[i];
+    for ( uint32_t s = 0; s < a.n_split; ++s ) u += a.split_flags[( size_t ) s * a.n + i];
+    const uint32_t v = a.v_acc[i];
+    if ( a.u_out ) { a.u_out[i] = u; a.v_out[i] = v; return; }
+    a.mark[i] = ( u >= 1 && u <= a.nseq && a.qok[u] && v >= a.nmin && v <= a.nmax ) ? 1 : 0;
+    a.rec_u[i] = u;
+    a.rec_v[i] = v;
+}
+
+} // namespace mtx

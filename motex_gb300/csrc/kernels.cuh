@@ -74,8 +74,54 @@ __global__ void k_finalize ( FinalizeArgs a );
 __global__ void k_compact ( const uint8_t * mark, const uint32_t * pref, uint32_t n, const uint32_t * rec_u,
                             const uint32_t * rec_v, uint32_t * out );
 
+// Structured motifs, two boxes / one gap (dp_struct.cu).
+struct StructArgs
+{
+    TextView          text;
+    const uint32_t *  wpl0;          // box-0 planes of the factor ending at each position: [b * total + pos]
+    const uint32_t *  wpl1;          // box-1 planes, same layout
+    const uint8_t *   row_ok;        // box 0 may end at this pattern position
+    const uint32_t *  row_end;       // end offset of the position's sequence
+    uint32_t          total;
+    uint32_t          l0, e0;        // box 0
+    uint32_t          l1, e1;        // box 1 (l1 = b1)
+    uint32_t          b1;
+    uint32_t          gmin, gmax, G; // gap range, G = gmax - gmin + 1
+    const ChunkInfo * chunks;
+    uint32_t *        u_acc;         // [pos * G + k]
+    uint32_t *        v_acc;
+    uint8_t *         split_flags;   // n_split rows of total * G bytes
+};
+
+struct StructFinalizeArgs
+{
+    uint64_t          n;             // total * G
+    const uint32_t *  u_acc;
+    const uint32_t *  v_acc;
+    const uint8_t *   split_flags;
+    uint32_t          n_split;
+    const uint8_t *   qok;
+    uint32_t          nseq, nmin, nmax;
+    uint8_t *         mark;
+    uint32_t *        rec_u;
+    uint32_t *        rec_v;
+    uint32_t *        u_out;         // pair mode: totals out
+    uint32_t *        v_out;
+};
+
+bool launch_dp_struct1 ( const StructArgs & a, int B, bool ed, dim3 grid, cudaStream_t st );
+__global__ void k_wplanes_all ( const uint8_t * codes, uint32_t total, uint32_t l, uint32_t B, int top_aligned,
+                                uint32_t * out );
+__global__ void k_struct_rows ( const uint32_t * offs, uint32_t nseq, uint64_t total, uint32_t l0, uint32_t tml,
+                                int pair_mode, uint8_t * row_ok, uint32_t * row_end );
+__global__ void k_struct_finalize ( StructFinalizeArgs a );
+
 // DP launchers (dp.cu): return false if no kernel matches the shape.
-bool launch_dp_fast ( const DPArgs & a, int B, int W, bool ed, dim3 grid, cudaStream_t st );
+bool launch_dp_fast ( const DPArgs & a, int B, int W, int UR, bool ed, dim3 grid, cudaStream_t st );
+// Edit distance, NL = swar_lanes(l) >= 2 factors per 32-bit register (l <= 15);
+// dynamic shared memory 3 * W * NL * kDPThreads words.
+int swar_lanes ( uint32_t l );
+bool launch_dp_swar_ed ( const DPArgs & a, int B, int NL, int W, int UR, dim3 grid, cudaStream_t st );
 bool launch_dp_generic ( const DPArgs & a, int B, uint32_t nw64, bool ed, dim3 grid, cudaStream_t st );
 
 } // namespace mtx

@@ -13,6 +13,7 @@
 #include <cstring>
 #include <map>
 #include <string>
+#include <unordered_set>
 #include <vector>
 
 using namespace mtx;
@@ -58,10 +59,17 @@ enum Slot
     S_RAW, S_OFFS, S_WSTART, S_QOK, S_CMAP, S_PRESENT, S_CODES, S_PLANES, S_VMASK, S_EMASK,
     S_WPOS, S_KEY0, S_KEY1, S_IDX1, S_HIST, S_HEAD, S_PREF, S_UNIQ, S_WPL32, S_WPL64,
     S_CHUNKS, S_UACC, S_VACC, S_FLAGS, S_MARK, S_RECU, S_RECV, S_PREF2, S_RECS, S_TILES,
-    S_SCALAR, S_UOUT, S_VOUT, S_COUNT
+    S_SCALAR, S_UOUT, S_VOUT, S_WPL0, S_WPL1, S_ROWOK, S_ROWEND, S_COUNT
 };
 
 } // namespace
+
+struct DPTune
+{
+    int W = 8;     // register words per thread
+    int NL = 1;    // factors per register word
+    int UR = 8;    // unroll of the 32-position block
+};
 
 struct motex_ctx
 {
@@ -86,12 +94,15 @@ struct motex_ctx
     uint32_t nwords = 0;
     bool pair_mode = false;
     uint64_t ref_cells = 0;
+    uint32_t G = 1;                            // gap choices (1 for single motifs)
+    std::vector<char> raw_host;                // structured runs: input copy for key dedup
 
     // executed job
     int B = 0;
     uint32_t U = 0, nblk = 0, n_split = 0, nrec = 0;
     uint64_t exec_cells = 0;
     float device_ms = 0.f, dp_ms = 0.f;
+    DPTune tune;
 };
 
 namespace
@@ -163,7 +174,18 @@ int validate ( const motex_params * p )
     if ( p->e >= p->l ) return fail ( MOTEX_EINVAL, "e must be less than the factor length" );
     if ( p->l > MOTEX_MAX_FACTOR ) return fail ( MOTEX_EUNSUPPORTED, "factor length %u > %d", p->l, MOTEX_MAX_FACTOR );
     if ( p->nb_gaps )
-        return fail ( MOTEX_EUNSUPPORTED, "structured motifs are not available in this entry point" );
+    {
+        if ( ! p->gap_min || ! p->gap_max || ! p->blens || ! p->berrs ) return fail ( MOTEX_EINVAL, "null box arrays" );
+        if ( p->nb_gaps > 1 )
+            return fail ( MOTEX_EUNSUPPORTED, "structured motifs with %u gaps (one gap is implemented)", p->nb_gaps );
+        const uint32_t gmin = p->gap_min[0], gmax = p->gap_max[0], b1 = p->blens[0];
+        if ( gmax < gmin ) return fail ( MOTEX_EINVAL, "gap range [%u,%u] is empty", gmin, gmax );
+        if ( b1 == 0 ) return fail ( MOTEX_EINVAL, "box length must be positive" );
+        if ( p->l > 32 || b1 > 32 || gmax - gmin + 1 > 32 || gmax + b1 > 31 )
+            return fail ( MOTEX_EUNSUPPORTED, "structured boxes need l, box length <= 32, gap max + box length <= 31 and at most 32 gap choices" );
+        if ( p->berrs[0] >= p->l + gmin + b1 )
+            return fail ( MOTEX_EUNSUPPORTED, "box error bound %u not below the minimum motif length", p->berrs[0] );
+    }
     return MOTEX_OK;
 }
 
@@ -209,6 +231,32 @@ int sort_factors ( motex_ctx * c, uint32_t n, uint32_t ** idx_out )
     }
     *idx_out = iin;
     return MOTEX_OK;
+}
+
+/*
+ * DP launch shape: factors per thread (W), factors per 32-bit register (NL,
+ * edit distance with l <= 15 packs 2-4), and the inner unroll of the
+ * 32-position text block (UR, bounded to keep the loop in the instruction
+ * cache).  MOTEX_DP_W / MOTEX_DP_UR / MOTEX_DP_SWAR=0 override the choice.
+ */
+DPTune choose_tune ( motex_ctx * c, uint32_t U, bool ed, bool generic )
+{
+    DPTune t;
+    if ( generic ) { t.W = 1; t.NL = 1; t.UR = 32; return t; }
+    t.NL = ed ? swar_lanes ( c->prm.l ) : 1;
+    const uint32_t groups = ( U + t.NL - 1 ) / t.NL;
+    t.W = groups >= ( uint32_t ) c->num_sms * kDPThreads * 8 ? 8 : 4;
+    t.UR = ed ? 8 : 4;             // measured on GB300: Hamming prefers the shorter body
+    if ( const char * e = getenv ( "MOTEX_DP_SWAR" ) )
+        if ( atoi ( e ) == 0 ) t.NL = 1;
+    if ( const char * e = getenv ( "MOTEX_DP_W" ) )
+        if ( atoi ( e ) == 4 || atoi ( e ) == 8 ) t.W = atoi ( e );
+    if ( const char * e = getenv ( "MOTEX_DP_UR" ) )
+    {
+        const int v = atoi ( e );
+        if ( v == 4 || v == 8 || ( v == 32 && t.NL == 1 ) ) t.UR = v;
+    }
+    return t;
 }
 
 /*
@@ -263,6 +311,132 @@ void build_chunks ( motex_ctx * c, uint32_t first_blk, uint32_t nchunks, uint32_
     c->n_split = ( uint32_t ) split_of.size ();
 }
 
+/*
+ * Structured motifs (one gap): box planes for every pattern position, the
+ * two-box DP over (pattern position x text chunk), then per (position, gap
+ * choice) filter and ordered compaction.  Factors are not deduplicated here:
+ * u and v are computed per pattern position like the reference, and the
+ * key deduplication of the writer happens on the passing entries only.
+ */
+int run_structured ( motex_ctx * c, const uint8_t * codes, uint32_t * planes, uint32_t stride, uint32_t * vmask,
+                     uint32_t * emask, uint32_t * scalar, uint32_t * h_scalar, bool & dp_timed )
+{
+    const motex_params & P = c->prm;
+    const bool ed = P.d == 1;
+    cudaStream_t st = c->st;
+    const int B = c->B;
+    const uint32_t T = ( uint32_t ) c->total, G = c->G;
+    const uint32_t b1 = c->blens[0], e1 = c->berrs[0], gmin = c->gmin[0], gmax = c->gmax[0];
+    uint32_t *wpl0, *wpl1, *row_end;
+    uint8_t * row_ok;
+    MTX_TRY ( ensure ( c, S_WPL0, ( size_t ) B * T, &wpl0 ) );
+    MTX_TRY ( ensure ( c, S_WPL1, ( size_t ) B * T, &wpl1 ) );
+    MTX_TRY ( ensure ( c, S_ROWOK, T, &row_ok ) );
+    MTX_TRY ( ensure ( c, S_ROWEND, T, &row_end ) );
+    MTX_LAUNCH ( k_wplanes_all, blocks_for ( T, 256 ), 256, codes, T, P.l, ( uint32_t ) B, ed ? 0 : 1, wpl0 );
+    MTX_LAUNCH ( k_wplanes_all, blocks_for ( T, 256 ), 256, codes, T, b1, ( uint32_t ) B, ed ? 0 : 1, wpl1 );
+    MTX_LAUNCH ( k_struct_rows, blocks_for ( T, 256 ), 256, dptr<uint32_t> ( c, S_OFFS ), c->nseq, c->total, P.l,
+                 c->tml, ( int ) c->pair_mode, row_ok, row_end );
+
+    const uint32_t ctas_x = ( T + kDPThreads - 1 ) / kDPThreads;
+    const uint32_t first_blk = c->pair_mode ? ( c->offs[1] / 32 ) : 0;
+    const uint32_t warmup = ( ed ? std::max ( P.l + P.e - 1, b1 + e1 - 1 ) : 0 ) + gmax + b1;
+    uint32_t nchunks = std::max<uint32_t> ( 1, ( ( uint32_t ) c->num_sms * 24 + ctas_x - 1 ) / ctas_x );
+    nchunks = std::min<uint32_t> ( nchunks, std::max<uint32_t> ( 1, ( c->nblk - first_blk ) / 16 ) );
+    nchunks = std::min<uint32_t> ( nchunks, 2048 );
+    std::vector<ChunkInfo> chunks;
+    build_chunks ( c, first_blk, nchunks, warmup, chunks );
+    ChunkInfo * h_chunks = reinterpret_cast<ChunkInfo *> ( static_cast<uint8_t *> ( c->pinned ) + 4096 );
+    std::copy ( chunks.begin (), chunks.end (), h_chunks );
+    ChunkInfo * d_chunks;
+    MTX_TRY ( ensure ( c, S_CHUNKS, chunks.size (), &d_chunks ) );
+    MTX_CUDA ( cudaMemcpyAsync ( d_chunks, h_chunks, chunks.size () * sizeof ( ChunkInfo ), cudaMemcpyHostToDevice, st ) );
+    uint64_t scanned = 0;
+    for ( auto & ch : chunks ) scanned += ( uint64_t ) ( ch.end - ch.warm ) * 32;
+    c->exec_cells = ( uint64_t ) T * scanned * 2;
+
+    const uint64_t n = ( uint64_t ) T * G;
+    if ( n >= 0xffffff00ull ) return fail ( MOTEX_EUNSUPPORTED, "positions x gap choices exceeds 2^32" );
+    uint32_t *u_acc, *v_acc;
+    uint8_t * flags;
+    MTX_TRY ( ensure ( c, S_UACC, n, &u_acc ) );
+    MTX_TRY ( ensure ( c, S_VACC, n, &v_acc ) );
+    MTX_TRY ( ensure ( c, S_FLAGS, std::max<uint64_t> ( 1, c->n_split ) * n, &flags ) );
+    MTX_CUDA ( cudaMemsetAsync ( u_acc, 0, n * 4, st ) );
+    MTX_CUDA ( cudaMemsetAsync ( v_acc, 0, n * 4, st ) );
+    if ( c->n_split ) MTX_CUDA ( cudaMemsetAsync ( flags, 0, ( size_t ) c->n_split * n, st ) );
+
+    StructArgs sa;
+    sa.text.planes = planes;
+    sa.text.plane_stride = stride;
+    sa.text.vmask = vmask;
+    sa.text.emask = emask;
+    sa.text.nblk = c->nblk;
+    sa.wpl0 = wpl0;
+    sa.wpl1 = wpl1;
+    sa.row_ok = row_ok;
+    sa.row_end = row_end;
+    sa.total = T;
+    sa.l0 = P.l;
+    sa.e0 = P.e;
+    sa.l1 = b1;
+    sa.e1 = e1;
+    sa.b1 = b1;
+    sa.gmin = gmin;
+    sa.gmax = gmax;
+    sa.G = G;
+    sa.chunks = d_chunks;
+    sa.u_acc = u_acc;
+    sa.v_acc = v_acc;
+    sa.split_flags = flags;
+    MTX_CUDA ( cudaEventRecord ( c->evd0, st ) );
+    if ( ! launch_dp_struct1 ( sa, B, ed, dim3 ( ctas_x, ( unsigned ) chunks.size () ), st ) )
+        return fail ( MOTEX_EUNSUPPORTED, "no structured DP kernel for this box shape" );
+    MTX_TRY ( check_launch ( c, "k_dp_struct1" ) );
+    MTX_CUDA ( cudaEventRecord ( c->evd1, st ) );
+    dp_timed = true;
+    c->U = T;
+
+    StructFinalizeArgs fa {};
+    fa.n = n;
+    fa.u_acc = u_acc;
+    fa.v_acc = v_acc;
+    fa.split_flags = flags;
+    fa.n_split = c->n_split;
+    fa.qok = dptr<uint8_t> ( c, S_QOK );
+    fa.nseq = c->nseq;
+    fa.nmin = P.n;
+    fa.nmax = P.N;
+    if ( c->pair_mode )
+    {
+        uint32_t *uo, *vo;
+        MTX_TRY ( ensure ( c, S_UOUT, n, &uo ) );
+        MTX_TRY ( ensure ( c, S_VOUT, n, &vo ) );
+        fa.u_out = uo;
+        fa.v_out = vo;
+        MTX_LAUNCH ( k_struct_finalize, blocks_for ( n, 256 ), 256, fa );
+        c->nrec = 0;
+        return MOTEX_OK;
+    }
+    uint8_t * mark;
+    uint32_t *recu, *recv, *pref2, *recs;
+    MTX_TRY ( ensure ( c, S_MARK, n, &mark ) );
+    MTX_TRY ( ensure ( c, S_RECU, n, &recu ) );
+    MTX_TRY ( ensure ( c, S_RECV, n, &recv ) );
+    MTX_TRY ( ensure ( c, S_PREF2, n, &pref2 ) );
+    fa.mark = mark;
+    fa.rec_u = recu;
+    fa.rec_v = recv;
+    MTX_LAUNCH ( k_struct_finalize, blocks_for ( n, 256 ), 256, fa );
+    MTX_TRY ( scan_flags ( c, mark, ( uint32_t ) n, pref2, scalar ) );
+    MTX_CUDA ( cudaMemcpyAsync ( h_scalar, scalar, 4, cudaMemcpyDeviceToHost, st ) );
+    MTX_CUDA ( cudaStreamSynchronize ( st ) );
+    c->nrec = h_scalar[0];
+    MTX_TRY ( ensure ( c, S_RECS, ( size_t ) 3 * std::max<uint32_t> ( 1, c->nrec ), &recs ) );
+    MTX_LAUNCH ( k_compact, blocks_for ( n, 256 ), 256, mark, pref2, ( uint32_t ) n, recu, recv, recs );
+    return MOTEX_OK;
+}
+
 int run_pipeline ( motex_ctx * c )
 {
     const motex_params & P = c->prm;
@@ -282,7 +456,7 @@ int run_pipeline ( motex_ctx * c )
     uint8_t * h_cmap = static_cast<uint8_t *> ( c->pinned ) + 1024;
     uint32_t sigma = 0;
     for ( int i = 0; i < 256; ++i ) h_cmap[i] = h_present[i] ? ( uint8_t ) sigma++ : 0;
-    int B = 1;
+    int B = 2;                                   // one- and two-symbol inputs run on the 2-plane kernels
     while ( ( 1u << B ) < sigma ) ++B;
     if ( B > kMaxPlanes ) return fail ( MOTEX_EUNSUPPORTED, "%u distinct symbols need %d bit planes (max %d)", sigma, B, kMaxPlanes );
     c->B = B;
@@ -323,12 +497,26 @@ int run_pipeline ( motex_ctx * c )
     pa.nblk = c->nblk;
     MTX_LAUNCH ( k_pack, std::min<unsigned> ( 16 * c->num_sms, blocks_for ( c->nblk, 8 ) ), 256, pa );
 
-    // dedup (whole-set runs); the pair drop-in searches every factor as is
-    uint32_t * uniq = wpos;
-    c->U = c->nwords;
     uint32_t * scalar;
     MTX_TRY ( ensure ( c, S_SCALAR, 4, &scalar ) );
     uint32_t * h_scalar = reinterpret_cast<uint32_t *> ( static_cast<uint8_t *> ( c->pinned ) + 2048 );
+    c->n_split = 0;
+    c->exec_cells = 0;
+    c->dp_ms = 0.f;
+    if ( P.nb_gaps )
+    {
+        bool timed = false;
+        MTX_TRY ( run_structured ( c, codes, planes, stride, vmask, emask, scalar, h_scalar, timed ) );
+        MTX_CUDA ( cudaEventRecord ( c->ev1, st ) );
+        MTX_CUDA ( cudaEventSynchronize ( c->ev1 ) );
+        MTX_CUDA ( cudaEventElapsedTime ( &c->device_ms, c->ev0, c->ev1 ) );
+        if ( timed ) MTX_CUDA ( cudaEventElapsedTime ( &c->dp_ms, c->evd0, c->evd1 ) );
+        return MOTEX_OK;
+    }
+
+    // dedup (whole-set runs); the pair drop-in searches every factor as is
+    uint32_t * uniq = wpos;
+    c->U = c->nwords;
     if ( ! c->pair_mode && c->nwords > 0 )
     {
         uint32_t * idx;
@@ -350,9 +538,6 @@ int run_pipeline ( motex_ctx * c )
     uint32_t *u_acc, *v_acc;
     MTX_TRY ( ensure ( c, S_UACC, U, &u_acc ) );
     MTX_TRY ( ensure ( c, S_VACC, U, &v_acc ) );
-    c->n_split = 0;
-    c->exec_cells = 0;
-    c->dp_ms = 0.f;
     bool dp_timed = false;
     if ( U > 0 )
     {
@@ -368,9 +553,11 @@ int run_pipeline ( motex_ctx * c )
         da.e = P.e;
         da.wplanes32 = nullptr;
         da.wplanes64 = nullptr;
-        const int W = generic ? 1 : ( U >= ( uint32_t ) c->num_sms * kDPThreads * 8 ? 8 : 4 );
+        const DPTune tune = choose_tune ( c, U, ed, generic );
+        const int W = tune.W;
+        const uint32_t groups = ( U + tune.NL - 1 ) / tune.NL;        // factors per register: NL
         const uint32_t per_cta = ( uint32_t ) kDPThreads * W;
-        const uint32_t ntiles = ( U + per_cta - 1 ) / per_cta;
+        const uint32_t ntiles = ( groups + per_cta - 1 ) / per_cta;
         uint32_t nw64 = ( P.l + 63 ) / 64;
         if ( ! generic )
         {
@@ -414,7 +601,10 @@ int run_pipeline ( motex_ctx * c )
         da.split_flags = flags;
         dim3 grid ( generic ? ( U + kDPThreads - 1 ) / kDPThreads : ntiles, ( unsigned ) chunks.size () );
         MTX_CUDA ( cudaEventRecord ( c->evd0, st ) );
-        bool ok = generic ? launch_dp_generic ( da, B, nw64, ed, grid, st ) : launch_dp_fast ( da, B, W, ed, grid, st );
+        bool ok = generic        ? launch_dp_generic ( da, B, nw64, ed, grid, st )
+                  : tune.NL > 1  ? launch_dp_swar_ed ( da, B, tune.NL, W, tune.UR, grid, st )
+                                 : launch_dp_fast ( da, B, W, tune.UR, ed, grid, st );
+        c->tune = tune;
         if ( ! ok ) return fail ( MOTEX_EUNSUPPORTED, "no DP kernel for l=%u B=%d", P.l, B );
         MTX_TRY ( check_launch ( c, "k_dp" ) );
         MTX_CUDA ( cudaEventRecord ( c->evd1, st ) );
@@ -479,7 +669,15 @@ int load_common ( motex_ctx * c, const motex_params * prm, const char * const * 
     if ( nseq == 0 ) return fail ( MOTEX_EINVAL, "no sequences" );
     c->loaded = c->executed = false;
     c->prm = *prm;
-    c->prm.gap_min = c->prm.gap_max = c->prm.blens = c->prm.berrs = nullptr;
+    c->gmin.assign ( prm->gap_min, prm->gap_min + prm->nb_gaps );
+    c->gmax.assign ( prm->gap_max, prm->gap_max + prm->nb_gaps );
+    c->blens.assign ( prm->blens, prm->blens + prm->nb_gaps );
+    c->berrs.assign ( prm->berrs, prm->berrs + prm->nb_gaps );
+    c->prm.gap_min = c->gmin.data ();
+    c->prm.gap_max = c->gmax.data ();
+    c->prm.blens = c->blens.data ();
+    c->prm.berrs = c->berrs.data ();
+    c->G = prm->nb_gaps ? c->gmax[0] - c->gmin[0] + 1 : 1;
     c->nseq = nseq;
     c->pair_mode = pair_mode;
     c->offs.assign ( nseq + 1, 0 );
@@ -495,7 +693,10 @@ int load_common ( motex_ctx * c, const motex_params * prm, const char * const * 
     c->total = total;
     if ( total == 0 ) return fail ( MOTEX_EINVAL, "empty input" );
     const uint32_t l = prm->l;
-    c->tml = pair_mode ? 0 : l;                   // total_mot_length of the plain search (motex.cc:360)
+    // total_mot_length (motex.cc:312-360): l plus minimum gaps and boxes
+    uint32_t tml_full = l;
+    for ( uint32_t g = 0; g < prm->nb_gaps; ++g ) tml_full += c->gmin[g] + c->blens[g];
+    c->tml = pair_mode ? 0 : tml_full;
     // factor ends per sequence and the reference's cell count
     std::vector<uint32_t> wstart ( nseq + 1, 0 );
     uint64_t nw = 0, searched = 0;
@@ -508,7 +709,7 @@ int load_common ( motex_ctx * c, const motex_params * prm, const char * const * 
     }
     wstart[nseq] = ( uint32_t ) nw;
     c->nwords = ( uint32_t ) nw;
-    c->ref_cells = pair_mode ? ( uint64_t ) lens[0] * lens[1] : searched * searched;
+    c->ref_cells = ( pair_mode ? ( uint64_t ) lens[0] * lens[1] : searched * searched ) * ( prm->nb_gaps + 1 );
     // qok[u]: the reference's double-precision quorum test (functions.cc:1105-1108)
     std::vector<uint8_t> qok ( nseq + 1 );
     for ( uint32_t u = 0; u <= nseq; ++u )
@@ -527,6 +728,8 @@ int load_common ( motex_ctx * c, const motex_params * prm, const char * const * 
         memcpy ( stage + at, seqs[i], lens[i] );
         at += lens[i];
     }
+    if ( prm->nb_gaps && ! pair_mode ) c->raw_host.assign ( stage, stage + total );
+    else c->raw_host.clear ();
     memcpy ( stage + raw_b, c->offs.data (), ( size_t ) ( nseq + 1 ) * 4 );
     memcpy ( stage + raw_b + offs_b, wstart.data (), ( size_t ) ( nseq + 1 ) * 4 );
     memcpy ( stage + raw_b + 2 * offs_b, qok.data (), nseq + 1 );
@@ -564,14 +767,28 @@ int fetch_records ( motex_ctx * c, motex_result * out )
     MTX_CUDA ( cudaStreamSynchronize ( c->st ) );
     out->motifs = static_cast<motex_motif *> ( malloc ( ( size_t ) c->nrec * sizeof ( motex_motif ) ) );
     if ( ! out->motifs ) return fail ( MOTEX_ENOMEM, "host allocation of the result failed" );
-    uint32_t s = 0;
+    const uint32_t G = c->prm.nb_gaps ? c->G : 1;
+    std::unordered_set<std::string> seen;
+    std::string key;
+    uint32_t s = 0, kept = 0;
     for ( uint32_t i = 0; i < c->nrec; ++i )
     {
-        const uint32_t pos = h[3 * i];
-        while ( c->offs[s + 1] <= pos ) ++s;        // records are in position order
-        out->motifs[i] = motex_motif { s, pos - c->offs[s], 0, h[3 * i + 1], h[3 * i + 2] };
+        const uint32_t idx = h[3 * i];
+        const uint32_t pos = idx / G, k = idx % G;
+        while ( c->offs[s + 1] <= pos ) ++s;        // records are in (position, gap choice) order
+        if ( c->prm.nb_gaps )
+        {
+            // the writer's key: box 0 and box 1 joined by '_', gap left out
+            // (functions.cc:1191-1239); the first passing entry of a key wins
+            const uint32_t l = c->prm.l, b1 = c->blens[0], gap = c->gmin[0] + k;
+            key.assign ( c->raw_host.data () + pos + 1 - l, l );
+            key.push_back ( '_' );
+            key.append ( c->raw_host.data () + pos + 1 + gap, b1 );
+            if ( ! seen.insert ( key ).second ) continue;
+        }
+        out->motifs[kept++] = motex_motif { s, pos - c->offs[s], k, h[3 * i + 1], h[3 * i + 2] };
     }
-    out->count = c->nrec;
+    out->count = kept;
     return MOTEX_OK;
 }
 
@@ -687,6 +904,26 @@ int motex_gpu_extract_pair ( motex_ctx * c, const motex_params * prm, const char
     MTX_TRY ( load_common ( c, prm, seqs, lens, 2, true ) );
     c->job_launches = 0;
     MTX_TRY ( run_pipeline ( c ) );
+    if ( prm->nb_gaps )
+    {
+        // per (position of p, gap choice k): u[k*m + j] (functions.cc:676-684)
+        const uint32_t G = c->G;
+        const size_t bytes = ( size_t ) m * G * 4;
+        MTX_TRY ( ensure_pinned ( c, 2 * bytes + 65536 ) );
+        uint32_t * hu = static_cast<uint32_t *> ( c->pinned );
+        uint32_t * hv = hu + ( size_t ) m * G;
+        MTX_CUDA ( cudaMemcpyAsync ( hu, dptr<uint32_t> ( c, S_UOUT ), bytes, cudaMemcpyDeviceToHost, c->st ) );
+        MTX_CUDA ( cudaMemcpyAsync ( hv, dptr<uint32_t> ( c, S_VOUT ), bytes, cudaMemcpyDeviceToHost, c->st ) );
+        MTX_CUDA ( cudaStreamSynchronize ( c->st ) );
+        for ( uint32_t j = 0; j < m; ++j )
+            for ( uint32_t k = 0; k < G; ++k )
+            {
+                u[( size_t ) k * m + j] += hu[( size_t ) j * G + k];
+                v[( size_t ) k * m + j] += hv[( size_t ) j * G + k];
+            }
+        c->loaded = false;
+        return MOTEX_OK;
+    }
     const uint32_t U = c->U;
     const size_t bytes = ( size_t ) U * 4;
     MTX_TRY ( ensure_pinned ( c, 2 * bytes + 65536 ) );

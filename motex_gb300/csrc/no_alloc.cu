@@ -189,7 +189,7 @@ extern "C" int motex_gpu_extract_pair_static ( const motex_params * prm, const c
         am.code[( uint8_t ) *a] = ( uint8_t ) sigma++;
     }
     if ( sigma == 0 ) return MOTEX_EINVAL;
-    int B = 1;
+    int B = 2;                                    // the DP kernels start at two bit planes
     while ( ( 1u << B ) < sigma ) ++B;
 
     int dev = 0;
@@ -246,7 +246,7 @@ extern "C" int motex_gpu_extract_pair_static ( const motex_params * prm, const c
     da.u_acc = u_acc;
     da.v_acc = v_acc;
     da.split_flags = flags;
-    if ( ! launch_dp_fast ( da, B, W, ed, dim3 ( ntiles, nchunks ), st ) ) return MOTEX_EUNSUPPORTED;
+    if ( ! launch_dp_fast ( da, B, W, 8, ed, dim3 ( ntiles, nchunks ), st ) ) return MOTEX_EUNSUPPORTED;
     k_na_accumulate<<<( U + 255 ) / 256, 256, 0, st>>> ( u_acc, v_acc, flags, nchunks > 1, U, l, err, d_u, d_v );
     if ( cudaGetLastError () != cudaSuccess ) return MOTEX_ECUDA;
     // report symbols outside the alphabet (the outputs were left untouched)

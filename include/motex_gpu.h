@@ -133,12 +133,32 @@ void motex_result_free ( motex_result * res );
  * the GPU across extractions: motex_gpu_load() uploads and packs the
  * sequences once; motex_gpu_execute() runs the extraction on the resident
  * input and leaves the result on the device; motex_gpu_fetch() copies it
- * back.  load + execute + fetch == run.
+ * back.  load + execute + fetch == run.  From the second execute of the same
+ * loaded input on, the whole device sequence is replayed as one CUDA graph.
  */
 int motex_gpu_load ( motex_ctx * ctx, const motex_params * prm,
                      const char * const * seqs, const uint32_t * lens, uint32_t nseq );
 int motex_gpu_execute ( motex_ctx * ctx );
 int motex_gpu_fetch ( motex_ctx * ctx, motex_result * out );
+
+/*
+ * Batched, uneven-size extraction: njobs independent whole-set extractions
+ * (each like motex_gpu_run, with its own sequences and parameters) walk the
+ * pipeline together; the factor-search DP of all single-motif jobs that share
+ * a kernel class runs as one persistent launch fed from a device work queue
+ * of (job, factor tile, text chunk) items, largest first.  results[i]
+ * receives job i's result (free each with motex_result_free); its dp_ms is
+ * the device time of the batch's shared DP launches.
+ */
+typedef struct motex_job
+{
+    const motex_params * prm;
+    const char * const * seqs;
+    const uint32_t *     lens;
+    uint32_t             nseq;
+} motex_job;
+
+int motex_gpu_run_batch ( motex_ctx * ctx, const motex_job * jobs, uint32_t njobs, motex_result * results );
 
 /*
  * Plain per-pair drop-in for

@@ -1,251 +1,17 @@
-// All-factors x all-texts approximate-matching DP of the GB300 engine.
-//
-// Every CTA owns kDPThreads * W searched factors (W per thread, bit planes in
-// registers) and one chunk of the concatenated text; all its threads walk the
-// same text positions, so the text stream is a broadcast read and every
-// per-position quantity is computed once per thread and reused by W factors.
-//
-//  Hamming (d = 0), flasm_hd contract: a hit ends at text position p when the
-//    window t[p-l+1..p] lies inside one sequence and has <= e mismatches.
-//    The 32 text symbols ending at p are one funnel shift of two plane words
-//    per plane; mismatches = OR over planes of (factor ^ window), masked to
-//    the top l bits; hit = popc <= e.
-//  Edit distance (d = 1), flasm_ed contract: a hit ends at p when
-//    min_s ED(factor, t[s..p]) <= e.  Myers/Hyyro bit-vector column recurrence
-//    (one 32-bit word per factor, l <= 32), Eq built from the factor planes
-//    and the broadcast text symbol bits; the score D[l][p] is tracked either
-//    scaled by 2^(l-1) (l <= 28, two ANDs and one add) or shifted down.
-//
-// Per (factor, sequence): hits are counted; at the end of each sequence the
-// count goes to v and (count > 0) to u.  A sequence cut by a chunk boundary
-// records its presence in a per-split-sequence flag row instead, so u counts
-// it once however many chunks saw it.
-#include "kernels.cuh"
+// All-factors x all-texts approximate-matching DP of the GB300 engine: static-
+// grid kernels (one job per launch) and their launchers.  The kernel bodies
+// and the design notes are in dp_body.cuh.
+#include "dp_body.cuh"
 
 #include <algorithm>
 
 namespace mtx
 {
 
-namespace
-{
-
-template <int W>
-__device__ __forceinline__ void flush_sequence ( const DPArgs & a, uint32_t base, int cur_split, uint32_t ( &cnt )[W],
-                                                 uint32_t ( &uacc )[W], uint32_t ( &vacc )[W] )
-{
-#pragma unroll
-    for ( int i = 0; i < W; ++i )
-    {
-        const uint32_t c = cnt[i];
-        if ( cur_split < 0 )
-            uacc[i] += c != 0u;
-        else if ( c )
-        {
-            const uint32_t w = base + i * kDPThreads;
-            if ( w < a.U ) a.split_flags[( size_t ) cur_split * a.U + w] = 1;
-        }
-        vacc[i] += c;
-        cnt[i] = 0;
-    }
-}
-
-template <int W>
-__device__ __forceinline__ void finish_chunk ( const DPArgs & a, const ChunkInfo & ch, uint32_t base,
-                                               uint32_t ( &cnt )[W], uint32_t ( &uacc )[W], uint32_t ( &vacc )[W] )
-{
-#pragma unroll
-    for ( int i = 0; i < W; ++i )
-    {
-        const uint32_t w = base + i * kDPThreads;
-        if ( w >= a.U ) continue;
-        const uint32_t c = cnt[i];
-        if ( c )
-        {
-            if ( ch.last_split >= 0 ) a.split_flags[( size_t ) ch.last_split * a.U + w] = 1;
-            else uacc[i] += 1;
-        }
-        const uint32_t v = vacc[i] + c;
-        if ( uacc[i] ) atomicAdd ( a.u_acc + w, uacc[i] );
-        if ( v ) atomicAdd ( a.v_acc + w, v );
-    }
-}
-
-} // namespace
-
 template <int B, int W, bool ED, bool SCALED, int UR>
 __global__ void __launch_bounds__ ( kDPThreads ) k_dp_fast ( const DPArgs a )
 {
-    const uint32_t base = blockIdx.x * ( kDPThreads * W ) + threadIdx.x;
-    const uint32_t l = a.l;
-    uint32_t wp[W][B];
-    uint32_t cnt[W], uacc[W], vacc[W];
-#pragma unroll
-    for ( int i = 0; i < W; ++i )
-    {
-        const uint32_t w = base + i * kDPThreads;
-        const bool ok = w < a.U;
-#pragma unroll
-        for ( int b = 0; b < B; ++b ) wp[i][b] = ok ? __ldg ( a.wplanes32 + ( size_t ) b * a.U + w ) : 0u;
-        cnt[i] = uacc[i] = vacc[i] = 0;
-    }
-    const ChunkInfo ch = a.chunks[blockIdx.y];
-    int cur_split = ch.first_split;
-    const uint32_t * __restrict__ planes = a.text.planes;
-    const uint32_t stride = a.text.plane_stride;
-
-    if constexpr ( ! ED )
-    {
-        const uint32_t topmask = l >= 32 ? 0xffffffffu : ~( ( 1u << ( 32 - l ) ) - 1u );
-        const uint32_t e = a.e;
-        uint32_t prev[B], cur[B];
-#pragma unroll
-        for ( int b = 0; b < B; ++b ) prev[b] = __ldg ( planes + ( size_t ) b * stride + ch.begin );
-        for ( uint32_t k = ch.begin; k < ch.end; ++k )
-        {
-#pragma unroll
-            for ( int b = 0; b < B; ++b ) cur[b] = __ldg ( planes + ( size_t ) b * stride + k + 1 );
-            const uint32_t vm = __ldg ( a.text.vmask + k ), em = __ldg ( a.text.emask + k );
-            if ( vm == 0xffffffffu && em == 0u )
-            {
-#pragma unroll 1
-                for ( int g = 0; g < 32; g += UR )
-                {
-#pragma unroll
-                    for ( int rr = 0; rr < UR; ++rr )
-                    {
-                        const int r = g + rr;
-                        uint32_t y[B];
-#pragma unroll
-                        for ( int b = 0; b < B; ++b ) y[b] = __funnelshift_rc ( prev[b], cur[b], r + 1 ) & topmask;
-#pragma unroll
-                        for ( int i = 0; i < W; ++i )
-                        {
-                            uint32_t x = wp[i][0] ^ y[0];
-#pragma unroll
-                            for ( int b = 1; b < B; ++b ) x |= wp[i][b] ^ y[b];
-                            cnt[i] += __popc ( x ) <= e;
-                        }
-                    }
-                }
-            }
-            else
-            {
-                for ( int r = 0; r < 32; ++r )
-                {
-                    if ( ( vm >> r ) & 1u )
-                    {
-                        uint32_t y[B];
-#pragma unroll
-                        for ( int b = 0; b < B; ++b ) y[b] = __funnelshift_rc ( prev[b], cur[b], r + 1 ) & topmask;
-#pragma unroll
-                        for ( int i = 0; i < W; ++i )
-                        {
-                            uint32_t x = wp[i][0] ^ y[0];
-#pragma unroll
-                            for ( int b = 1; b < B; ++b ) x |= wp[i][b] ^ y[b];
-                            cnt[i] += __popc ( x ) <= e;
-                        }
-                    }
-                    if ( ( em >> r ) & 1u )
-                    {
-                        flush_sequence<W> ( a, base, cur_split, cnt, uacc, vacc );
-                        cur_split = -1;
-                    }
-                }
-            }
-#pragma unroll
-            for ( int b = 0; b < B; ++b ) prev[b] = cur[b];
-        }
-    }
-    else
-    {
-        const uint32_t hb = 1u << ( l - 1 );
-        const uint32_t sc0 = SCALED ? ( l << ( l - 1 ) ) : l;
-        const uint32_t thr = SCALED ? ( ( a.e + 1 ) << ( l - 1 ) ) : ( a.e + 1 );
-        const uint32_t sh = l - 1;
-        uint32_t Pv[W], Mv[W], sc[W];
-#pragma unroll
-        for ( int i = 0; i < W; ++i ) { Pv[i] = 0xffffffffu; Mv[i] = 0; sc[i] = sc0; }
-
-        auto step = [&] ( int i, const uint32_t ( &T )[B] ) {
-            uint32_t x = wp[i][0] ^ T[0];
-#pragma unroll
-            for ( int b = 1; b < B; ++b ) x |= wp[i][b] ^ T[b];
-            const uint32_t Eq = ~x;
-            const uint32_t Xv = Eq | Mv[i];
-            const uint32_t Xh = ( ( ( Eq & Pv[i] ) + Pv[i] ) ^ Pv[i] ) | Eq;
-            uint32_t Ph = Mv[i] | ~( Xh | Pv[i] );
-            uint32_t Mh = Pv[i] & Xh;
-            if constexpr ( SCALED )
-                sc[i] += ( Ph & hb ) - ( Mh & hb );
-            else
-                sc[i] += ( ( Ph >> sh ) & 1u ) - ( ( Mh >> sh ) & 1u );
-            Ph <<= 1;
-            Mh <<= 1;
-            Pv[i] = Mh | ~( Xv | Ph );
-            Mv[i] = Ph & Xv;
-        };
-
-        uint32_t cur[B];
-        for ( uint32_t k = ch.warm; k < ch.end; ++k )
-        {
-#pragma unroll
-            for ( int b = 0; b < B; ++b ) cur[b] = __ldg ( planes + ( size_t ) b * stride + k + 1 );
-            const uint32_t vm = __ldg ( a.text.vmask + k ), em = __ldg ( a.text.emask + k );
-            const bool counting = k >= ch.begin;
-            if ( counting && vm == 0xffffffffu && em == 0u )
-            {
-#pragma unroll 1
-                for ( int g = 0; g < 32; g += UR )
-                {
-                    uint32_t cg[B];
-#pragma unroll
-                    for ( int b = 0; b < B; ++b ) cg[b] = cur[b] >> g;
-#pragma unroll
-                    for ( int rr = 0; rr < UR; ++rr )
-                    {
-                        uint32_t T[B];
-#pragma unroll
-                        for ( int b = 0; b < B; ++b ) T[b] = 0u - ( ( cg[b] >> rr ) & 1u );
-#pragma unroll
-                        for ( int i = 0; i < W; ++i )
-                        {
-                            step ( i, T );
-                            cnt[i] += sc[i] < thr;
-                        }
-                    }
-                }
-            }
-            else
-            {
-                for ( int r = 0; r < 32; ++r )
-                {
-                    uint32_t T[B];
-#pragma unroll
-                    for ( int b = 0; b < B; ++b ) T[b] = 0u - ( ( cur[b] >> r ) & 1u );
-                    const bool count_here = counting && ( ( vm >> r ) & 1u );
-#pragma unroll
-                    for ( int i = 0; i < W; ++i )
-                    {
-                        step ( i, T );
-                        if ( count_here ) cnt[i] += sc[i] < thr;
-                    }
-                    if ( ( em >> r ) & 1u )
-                    {
-                        if ( counting )
-                        {
-                            flush_sequence<W> ( a, base, cur_split, cnt, uacc, vacc );
-                            cur_split = -1;
-                        }
-#pragma unroll
-                        for ( int i = 0; i < W; ++i ) { Pv[i] = 0xffffffffu; Mv[i] = 0; sc[i] = sc0; }
-                    }
-                }
-            }
-        }
-    }
-    finish_chunk<W> ( a, ch, base, cnt, uacc, vacc );
+    dp_fast_body<B, W, ED, SCALED, UR> ( a, blockIdx.x, blockIdx.y );
 }
 
 /*
@@ -369,184 +135,10 @@ __global__ void __launch_bounds__ ( kDPThreads ) k_dp_generic ( const DPArgs a, 
     finish_chunk<1> ( a, ch, base, cnt, uacc, vacc );
 }
 
-/*
- * Edit distance with NL factors per 32-bit register (SWAR), l <= 15.
- * Lane i holds a factor in bits [i*S, i*S+l), S = l+1, with a guard bit at
- * i*S+l.  The text bits are cleared at the guards, so Eq has 1 there; Pv and
- * Mv keep 0 there (Mv through the NG mask, Pv because the Mh that is shifted
- * up is taken without the lanes' top bits).  With those invariants no carry
- * of (Eq&Pv)+Pv and no shifted Ph/Mh bit crosses into the next lane.  The
- * per-lane scores live in bit fields at i*S (each in [0, l]); the hit test
- * adds 2^(l-1)-(e+1) per field and reads bit l-1 of each field.  Hits are
- * counted in per-lane fields and moved to shared memory every 32 positions.
- */
-struct SwarConst
-{
-    uint32_t HB;     // bit l-1 of every lane
-    uint32_t NG;     // all bits but the guards
-    uint32_t NGm1;   // NG without the lanes' top bits
-    uint32_t K;      // per field 2^(l-1) - (e+1)
-    uint32_t SC0;    // per field score l
-    uint32_t S;      // lane stride
-    uint32_t FM;     // field mask (S bits)
-};
-
 template <int B, int NL, int W, int UR>
 __global__ void __launch_bounds__ ( kDPThreads ) k_dp_swar_ed ( const DPArgs a, const SwarConst C )
 {
-    extern __shared__ uint32_t smem[];
-    constexpr int NF = W * NL;                      // factors per thread
-    // [field][thread]: count in the current text, texts seen, occurrences
-    uint32_t * s_cnt = smem;
-    uint32_t * s_u = smem + NF * kDPThreads;
-    uint32_t * s_v = smem + 2 * NF * kDPThreads;
-    const int tid = threadIdx.x;
-    for ( int f = 0; f < NF; ++f ) s_cnt[f * kDPThreads + tid] = s_u[f * kDPThreads + tid] = s_v[f * kDPThreads + tid] = 0;
-
-    const uint32_t gbase = blockIdx.x * ( kDPThreads * W ) + tid;       // first factor group of this thread
-    const uint32_t l = a.l, sh = l - 1;
-    uint32_t wp[W][B];
-#pragma unroll
-    for ( int i = 0; i < W; ++i )
-    {
-#pragma unroll
-        for ( int b = 0; b < B; ++b ) wp[i][b] = 0;
-        const uint32_t g = gbase + i * kDPThreads;
-#pragma unroll
-        for ( int j = 0; j < NL; ++j )
-        {
-            const uint32_t w = g * NL + j;
-            if ( w < a.U )
-#pragma unroll
-                for ( int b = 0; b < B; ++b ) wp[i][b] |= __ldg ( a.wplanes32 + ( size_t ) b * a.U + w ) << ( j * C.S );
-        }
-    }
-    uint32_t Pv[W], Mv[W], sc[W], cnt[W];
-#pragma unroll
-    for ( int i = 0; i < W; ++i ) { Pv[i] = C.NG; Mv[i] = 0; sc[i] = C.SC0; cnt[i] = 0; }
-
-    const ChunkInfo ch = a.chunks[blockIdx.y];
-    int cur_split = ch.first_split;
-    const uint32_t * __restrict__ planes = a.text.planes;
-    const uint32_t stride = a.text.plane_stride;
-
-    auto step = [&] ( int i, const uint32_t ( &T )[B] ) {
-        uint32_t x = wp[i][0] ^ T[0];
-#pragma unroll
-        for ( int b = 1; b < B; ++b ) x |= wp[i][b] ^ T[b];
-        const uint32_t Xv = ~x | Mv[i];
-        const uint32_t s = ( ~x & Pv[i] ) + Pv[i];
-        const uint32_t Xh = ( s ^ Pv[i] ) | ~x;
-        const uint32_t Ph = Mv[i] | ~( Xh | Pv[i] );
-        const uint32_t Mhs = Pv[i] & Xh & C.NGm1;
-        const uint32_t mh = Pv[i] & Xh & C.HB;
-        const uint32_t ph = Ph & C.HB;
-        sc[i] = sc[i] + ( ph >> sh ) - ( mh >> sh );
-        const uint32_t Ph2 = Ph << 1, Mh2 = Mhs << 1;
-        Pv[i] = Mh2 | ~( Xv | Ph2 );
-        Mv[i] = Ph2 & Xv & C.NG;
-    };
-    auto count = [&] ( int i ) { cnt[i] += ( ~( sc[i] + C.K ) & C.HB ) >> sh; };
-    auto drain = [&] () {                           // register fields -> shared counters
-#pragma unroll
-        for ( int i = 0; i < W; ++i )
-        {
-#pragma unroll
-            for ( int j = 0; j < NL; ++j ) s_cnt[( i * NL + j ) * kDPThreads + tid] += ( cnt[i] >> ( j * C.S ) ) & C.FM;
-            cnt[i] = 0;
-        }
-    };
-    auto end_sequence = [&] () {
-        for ( int f = 0; f < NF; ++f )
-        {
-            const uint32_t c = s_cnt[f * kDPThreads + tid];
-            if ( ! c ) continue;
-            if ( cur_split < 0 ) s_u[f * kDPThreads + tid] += 1;
-            else
-            {
-                const uint32_t w = ( gbase + ( f / NL ) * kDPThreads ) * NL + ( f % NL );
-                if ( w < a.U ) a.split_flags[( size_t ) cur_split * a.U + w] = 1;
-            }
-            s_v[f * kDPThreads + tid] += c;
-            s_cnt[f * kDPThreads + tid] = 0;
-        }
-    };
-
-    for ( uint32_t k = ch.warm; k < ch.end; ++k )
-    {
-        uint32_t cur[B];
-#pragma unroll
-        for ( int b = 0; b < B; ++b ) cur[b] = __ldg ( planes + ( size_t ) b * stride + k + 1 );
-        const uint32_t vm = __ldg ( a.text.vmask + k ), em = __ldg ( a.text.emask + k );
-        const bool counting = k >= ch.begin;
-        if ( counting && vm == 0xffffffffu && em == 0u )
-        {
-#pragma unroll 1
-            for ( int g = 0; g < 32; g += UR )
-            {
-                uint32_t cg[B];
-#pragma unroll
-                for ( int b = 0; b < B; ++b ) cg[b] = cur[b] >> g;
-#pragma unroll
-                for ( int rr = 0; rr < UR; ++rr )
-                {
-                    uint32_t T[B];
-#pragma unroll
-                    for ( int b = 0; b < B; ++b ) T[b] = ( 0u - ( ( cg[b] >> rr ) & 1u ) ) & C.NG;
-#pragma unroll
-                    for ( int i = 0; i < W; ++i )
-                    {
-                        step ( i, T );
-                        count ( i );
-                    }
-                }
-            }
-        }
-        else
-        {
-            for ( int r = 0; r < 32; ++r )
-            {
-                uint32_t T[B];
-#pragma unroll
-                for ( int b = 0; b < B; ++b ) T[b] = ( 0u - ( ( cur[b] >> r ) & 1u ) ) & C.NG;
-                const bool count_here = counting && ( ( vm >> r ) & 1u );
-#pragma unroll
-                for ( int i = 0; i < W; ++i )
-                {
-                    step ( i, T );
-                    if ( count_here ) count ( i );
-                }
-                if ( ( em >> r ) & 1u )
-                {
-                    if ( counting )
-                    {
-                        drain ();
-                        end_sequence ();
-                        cur_split = -1;
-                    }
-#pragma unroll
-                    for ( int i = 0; i < W; ++i ) { Pv[i] = C.NG; Mv[i] = 0; sc[i] = C.SC0; }
-                }
-            }
-        }
-        drain ();
-    }
-    // chunk end
-    for ( int f = 0; f < NF; ++f )
-    {
-        const uint32_t w = ( gbase + ( f / NL ) * kDPThreads ) * NL + ( f % NL );
-        if ( w >= a.U ) continue;
-        const uint32_t c = s_cnt[f * kDPThreads + tid];
-        uint32_t u = s_u[f * kDPThreads + tid];
-        if ( c )
-        {
-            if ( ch.last_split >= 0 ) a.split_flags[( size_t ) ch.last_split * a.U + w] = 1;
-            else u += 1;
-        }
-        const uint32_t v = s_v[f * kDPThreads + tid] + c;
-        if ( u ) atomicAdd ( a.u_acc + w, u );
-        if ( v ) atomicAdd ( a.v_acc + w, v );
-    }
+    dp_swar_body<B, NL, W, UR> ( a, C, blockIdx.x, blockIdx.y );
 }
 
 // ------------------------------------------------------------------ launchers
@@ -611,8 +203,14 @@ static bool launch_swar_bnw ( const DPArgs & a, const SwarConst & C, int UR, dim
     const size_t smem = ( size_t ) 3 * W * NL * kDPThreads * sizeof ( uint32_t );
     switch ( UR )
     {
-        case 4: k_dp_swar_ed<B, NL, W, 4><<<grid, kDPThreads, smem, st>>> ( a, C ); return true;
-        case 8: k_dp_swar_ed<B, NL, W, 8><<<grid, kDPThreads, smem, st>>> ( a, C ); return true;
+        case 4:
+            cudaFuncSetAttribute ( k_dp_swar_ed<B, NL, W, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, ( int ) smem );
+            k_dp_swar_ed<B, NL, W, 4><<<grid, kDPThreads, smem, st>>> ( a, C );
+            return true;
+        case 8:
+            cudaFuncSetAttribute ( k_dp_swar_ed<B, NL, W, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, ( int ) smem );
+            k_dp_swar_ed<B, NL, W, 8><<<grid, kDPThreads, smem, st>>> ( a, C );
+            return true;
         default: return false;
     }
 }
@@ -640,10 +238,8 @@ static bool launch_swar_b ( const DPArgs & a, const SwarConst & C, int NL, int W
     }
 }
 
-bool launch_dp_swar_ed ( const DPArgs & a, int B, int NL, int W, int UR, dim3 grid, cudaStream_t st )
+SwarConst swar_const ( uint32_t l, uint32_t e, int NL )
 {
-    const uint32_t l = a.l;
-    if ( NL < 2 || NL != swar_lanes ( l ) ) return false;
     SwarConst C;
     C.S = l + 1;
     C.HB = C.NG = C.K = C.SC0 = 0;
@@ -653,12 +249,19 @@ bool launch_dp_swar_ed ( const DPArgs & a, int B, int NL, int W, int UR, dim3 gr
         const uint32_t o = j * C.S;
         C.HB |= 1u << ( o + l - 1 );
         if ( o + l < 32 ) guards |= 1u << ( o + l );
-        C.K += ( ( 1u << ( l - 1 ) ) - ( a.e + 1 ) ) << o;
+        C.K += ( ( 1u << ( l - 1 ) ) - ( e + 1 ) ) << o;
         C.SC0 += l << o;
     }
     C.NG = ~guards;
     C.NGm1 = C.NG & ~C.HB;
     C.FM = ( 1u << C.S ) - 1u;
+    return C;
+}
+
+bool launch_dp_swar_ed ( const DPArgs & a, int B, int NL, int W, int UR, dim3 grid, cudaStream_t st )
+{
+    if ( NL < 2 || NL != swar_lanes ( a.l ) ) return false;
+    const SwarConst C = swar_const ( a.l, a.e, NL );
     switch ( B )
     {
         case 1:

@@ -1,0 +1,112 @@
+// Persistent, batched form of the factor-search DP: one launch per kernel
+// class serves any number of jobs; CTAs pull (job, tile, chunk) items from a
+// device counter (see next_item in dp_body.cuh).
+#include "dp_body.cuh"
+
+namespace mtx
+{
+
+template <int B, int W, bool ED, bool SCALED, int UR>
+__global__ void __launch_bounds__ ( kDPThreads ) k_dp_fast_persist ( const JobDesc * jobs, const WorkItem * items,
+                                                                     uint32_t nitems, uint32_t * counter )
+{
+    WorkItem w;
+    while ( next_item ( items, nitems, counter, w ) )
+        dp_fast_body<B, W, ED, SCALED, UR> ( jobs[w.job].a, w.tile, w.chunk );
+}
+
+template <int B, int NL, int W, int UR>
+__global__ void __launch_bounds__ ( kDPThreads ) k_dp_swar_persist ( const JobDesc * jobs, const WorkItem * items,
+                                                                     uint32_t nitems, uint32_t * counter )
+{
+    WorkItem w;
+    while ( next_item ( items, nitems, counter, w ) )
+        dp_swar_body<B, NL, W, UR> ( jobs[w.job].a, jobs[w.job].C, w.tile, w.chunk );
+}
+
+namespace
+{
+
+template <typename K>
+int ctas_per_sm ( K kernel, size_t smem )
+{
+    int n = 0;
+    cudaFuncSetAttribute ( kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, ( int ) smem );
+    if ( cudaOccupancyMaxActiveBlocksPerMultiprocessor ( &n, kernel, kDPThreads, smem ) != cudaSuccess ) n = 1;
+    return n > 0 ? n : 1;
+}
+
+template <int B>
+bool launch_b ( const JobDesc * jobs, const WorkItem * items, uint32_t nitems, uint32_t * counter, bool ed, bool scaled,
+                int NL, unsigned grid, cudaStream_t st, int * occ )
+{
+    constexpr int W = 8;
+    if ( NL <= 1 )
+    {
+        if ( ! ed )
+        {
+            if ( occ ) { *occ = ctas_per_sm ( k_dp_fast_persist<B, W, false, false, 4>, 0 ); return true; }
+            k_dp_fast_persist<B, W, false, false, 4><<<grid, kDPThreads, 0, st>>> ( jobs, items, nitems, counter );
+        }
+        else if ( scaled )
+        {
+            if ( occ ) { *occ = ctas_per_sm ( k_dp_fast_persist<B, W, true, true, 8>, 0 ); return true; }
+            k_dp_fast_persist<B, W, true, true, 8><<<grid, kDPThreads, 0, st>>> ( jobs, items, nitems, counter );
+        }
+        else
+        {
+            if ( occ ) { *occ = ctas_per_sm ( k_dp_fast_persist<B, W, true, false, 8>, 0 ); return true; }
+            k_dp_fast_persist<B, W, true, false, 8><<<grid, kDPThreads, 0, st>>> ( jobs, items, nitems, counter );
+        }
+        return true;
+    }
+#define MTX_SWAR_P( NLV )                                                                                   \
+    case NLV:                                                                                               \
+    {                                                                                                       \
+        const size_t smem = ( size_t ) 3 * W * NLV * kDPThreads * sizeof ( uint32_t );                      \
+        if ( occ ) { *occ = ctas_per_sm ( k_dp_swar_persist<B, NLV, W, 8>, smem ); return true; }            \
+        cudaFuncSetAttribute ( k_dp_swar_persist<B, NLV, W, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize,   \
+                               ( int ) smem );                                                              \
+        k_dp_swar_persist<B, NLV, W, 8><<<grid, kDPThreads, smem, st>>> ( jobs, items, nitems, counter );     \
+        return true;                                                                                        \
+    }
+    switch ( NL )
+    {
+        MTX_SWAR_P ( 2 )
+        MTX_SWAR_P ( 3 )
+        MTX_SWAR_P ( 4 )
+        default: return false;
+    }
+#undef MTX_SWAR_P
+}
+
+bool dispatch ( const JobDesc * jobs, const WorkItem * items, uint32_t nitems, uint32_t * counter, int B, bool ed,
+                bool scaled, int NL, unsigned grid, cudaStream_t st, int * occ )
+{
+    switch ( B )
+    {
+        case 1:
+        case 2: return launch_b<2> ( jobs, items, nitems, counter, ed, scaled, NL, grid, st, occ );
+        case 3: return launch_b<3> ( jobs, items, nitems, counter, ed, scaled, NL, grid, st, occ );
+        case 4: return launch_b<4> ( jobs, items, nitems, counter, ed, scaled, NL, grid, st, occ );
+        case 5: return launch_b<5> ( jobs, items, nitems, counter, ed, scaled, NL, grid, st, occ );
+        default: return false;
+    }
+}
+
+} // namespace
+
+int persistent_ctas_per_sm ( int B, bool ed, bool scaled, int NL, int, int )
+{
+    int occ = 1;
+    if ( ! dispatch ( nullptr, nullptr, 0, nullptr, B, ed, scaled, NL, 0, nullptr, &occ ) ) return 1;
+    return occ;
+}
+
+bool launch_dp_persistent ( const JobDesc * jobs, const WorkItem * items, uint32_t nitems, uint32_t * counter, int B,
+                            bool ed, bool scaled, int NL, int, int, unsigned grid, cudaStream_t st )
+{
+    return dispatch ( jobs, items, nitems, counter, B, ed, scaled, NL, grid, st, nullptr );
+}
+
+} // namespace mtx

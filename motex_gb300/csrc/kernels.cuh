@@ -118,6 +118,36 @@ __global__ void k_struct_finalize ( StructFinalizeArgs a );
 
 // DP launchers (dp.cu): return false if no kernel matches the shape.
 bool launch_dp_fast ( const DPArgs & a, int B, int W, int UR, bool ed, dim3 grid, cudaStream_t st );
+// SWAR edit-distance lane constants (dp.cu).
+struct SwarConst
+{
+    uint32_t HB;     // bit l-1 of every lane
+    uint32_t NG;     // all bits but the guards
+    uint32_t NGm1;   // NG without the lanes' top bits
+    uint32_t K;      // per field 2^(l-1) - (e+1)
+    uint32_t SC0;    // per field score l
+    uint32_t S;      // lane stride
+    uint32_t FM;     // field mask (S bits)
+};
+SwarConst swar_const ( uint32_t l, uint32_t e, int NL );
+
+// One job of a batched launch and one unit of its work.
+struct JobDesc
+{
+    DPArgs    a;
+    SwarConst C;
+};
+struct WorkItem
+{
+    uint32_t job, tile, chunk;
+};
+
+// Persistent batched DP: kind 0 = 1-lane kernels (Hamming or edit distance),
+// kind 1 = SWAR edit distance with NL lanes.  grid = resident CTA slots.
+bool launch_dp_persistent ( const JobDesc * jobs, const WorkItem * items, uint32_t nitems, uint32_t * counter,
+                            int B, bool ed, bool scaled, int NL, int W, int UR, unsigned grid, cudaStream_t st );
+int persistent_ctas_per_sm ( int B, bool ed, bool scaled, int NL, int W, int UR );
+
 // Edit distance, NL = swar_lanes(l) >= 2 factors per 32-bit register (l <= 15);
 // dynamic shared memory 3 * W * NL * kDPThreads words.
 int swar_lanes ( uint32_t l );

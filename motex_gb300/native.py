@@ -23,7 +23,7 @@ EXPORTS = [
     "motex_ctx_create", "motex_ctx_destroy", "motex_gpu_run", "motex_result_free",
     "motex_gpu_load", "motex_gpu_execute", "motex_gpu_fetch", "motex_gpu_extract_pair",
     "motex_gpu_strerror", "motex_gpu_last_error", "motex_ctx_launches", "motex_probe_int_peak",
-    "motex_gpu_extract_pair_static",
+    "motex_gpu_extract_pair_static", "motex_gpu_run_batch",
 ]
 
 
@@ -38,6 +38,11 @@ class Params(C.Structure):
                 ("Q", C.c_uint32), ("n", C.c_uint32), ("N", C.c_uint32), ("nb_gaps", C.c_uint32),
                 ("gap_min", C.POINTER(C.c_uint32)), ("gap_max", C.POINTER(C.c_uint32)),
                 ("blens", C.POINTER(C.c_uint32)), ("berrs", C.POINTER(C.c_uint32))]
+
+
+class Job(C.Structure):
+    _fields_ = [("prm", C.POINTER(Params)), ("seqs", C.POINTER(C.c_char_p)), ("lens", C.POINTER(C.c_uint32)),
+                ("nseq", C.c_uint32)]
 
 
 class Motif(C.Structure):
@@ -77,6 +82,7 @@ def load_library(path: str = LIB_PATH):
         "motex_gpu_last_error": (C.c_char_p, []),
         "motex_ctx_launches": (C.c_uint64, [C.c_void_p]),
         "motex_probe_int_peak": (C.c_int, [C.c_int, P(C.c_double), P(C.c_double), P(C.c_double)]),
+        "motex_gpu_run_batch": (C.c_int, [C.c_void_p, P(Job), C.c_uint32, P(Result)]),
         "motex_gpu_extract_pair_static": (C.c_int, [P(Params), C.c_char_p, C.c_void_p, C.c_uint32, C.c_void_p,
                                                     C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p]),
     }
@@ -178,6 +184,22 @@ class Context:
             return self._collect(res)
         finally:
             self.lib.motex_result_free(C.byref(res))
+
+    def run_batch(self, jobs):
+        """jobs: list of (seqs, Params); returns one Extraction per job."""
+        keep = []
+        arr = (Job * len(jobs))()
+        for i, (seqs, prm) in enumerate(jobs):
+            bs, a, lens = self._seq_arrays(seqs)
+            keep.append((bs, a, lens, prm))
+            arr[i] = Job(C.pointer(prm), a, lens, len(bs))
+        res = (Result * len(jobs))()
+        _check(self.lib.motex_gpu_run_batch(self.h, arr, len(jobs), res))
+        out = []
+        for i in range(len(jobs)):
+            out.append(self._collect(res[i]))
+            self.lib.motex_result_free(C.byref(res[i]))
+        return out
 
     def load(self, seqs, params: Params):
         keep, arr, lens = self._seq_arrays(seqs)

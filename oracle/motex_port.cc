@@ -23,7 +23,8 @@
  * rejected with an error.
  *
  * Built twice: as the CLI binary (main) and, with -DMOTEX_PORT_LIB, as a
- * shared library exposing oracle_extract_pair() for fine-grained tests.
+ * shared library exposing oracle_extract_pair() and oracle_word_uv() for
+ * fine-grained tests.
  */
 #include "motex_core.h"
 
@@ -238,6 +239,27 @@ extern "C" int oracle_extract_pair ( int d, unsigned l, unsigned e, const char *
     if ( d == 1 ) build_peq ( C.seq[0], l, C.sigma, peq );
     std::vector<unsigned char> occ;
     extract_plain ( P, C.seq[0], C.seq[1], d == 1 ? &peq : nullptr, C.sigma, u, v, occ );
+    return 1;
+}
+
+/* u, v of one word over all searched sequences (length >= tml) of a set:
+ * the per-word totals the all-pairs driver accumulates (motex.cc:531-581). */
+extern "C" int oracle_word_uv ( int d, unsigned l, unsigned e, const char * word, const char * text,
+                                const unsigned * offs, unsigned nseq, unsigned tml, unsigned * u, unsigned * v )
+{
+    *u = *v = 0;
+    for ( unsigned s = 0; s < nseq; ++s )
+    {
+        const unsigned n = offs[s + 1] - offs[s];
+        if ( n < tml ) continue;
+        const unsigned char * t = ( const unsigned char * ) text + offs[s];
+        unsigned hits = 0;
+        auto on = [&] ( unsigned, unsigned, unsigned ) { hits++; };
+        if ( d == 0 ) hd_scan ( t, n, ( const unsigned char * ) word, l, l, e, on );
+        else ed_scan ( t, n, ( const unsigned char * ) word, l, l, e, on );
+        *u += hits > 0;
+        *v += hits;
+    }
     return 1;
 }
 

@@ -161,6 +161,56 @@ typedef struct motex_job
 int motex_gpu_run_batch ( motex_ctx * ctx, const motex_job * jobs, uint32_t njobs, motex_result * results );
 
 /*
+ * Serving: continuous batching of extraction requests (no counterpart in
+ * the reference, which extracts one input per process run).
+ *   motex_srv_create   starts `workers` worker threads on `device`, each
+ *                      with its own engine context and stream, so batches
+ *                      overlap on the GPU; hbm_budget_bytes bounds the
+ *                      estimated device working set of the requests in
+ *                      flight (0 = half of the free device memory);
+ *                      max_batch bounds requests per batch; max_queue bounds
+ *                      waiting requests (0 = unbounded).
+ *   motex_srv_submit   copies the request and queues it; MOTEX_ENOMEM if it
+ *                      can never fit the budget, MOTEX_EBUSY if the queue is
+ *                      full or the server is stopping.
+ *   motex_srv_wait     waits on the host up to timeout_ms (< 0: no limit)
+ *                      for request `id`; returns the request's own status,
+ *                      MOTEX_ETIMEOUT if it is still pending (it stays
+ *                      waitable), MOTEX_ENOTFOUND for unknown or collected
+ *                      ids.  The result's motif array belongs to the caller.
+ *   motex_srv_destroy  finishes the queued requests, then stops.
+ */
+typedef struct motex_server motex_server;
+
+typedef struct motex_srv_timing
+{
+    double   queue_ms;      /* submission -> batch admission */
+    double   run_ms;        /* batch admission -> results ready */
+    double   latency_ms;    /* submission -> results ready */
+    uint32_t batch_size;    /* requests in the batch that served it */
+} motex_srv_timing;
+
+typedef struct motex_srv_stats
+{
+    uint64_t submitted;
+    uint64_t completed;
+    uint64_t failed;
+    uint64_t batches;
+    uint64_t cells;         /* reference DP cells of completed requests */
+    uint32_t max_batch_seen;
+    uint32_t queued;
+    uint64_t in_use_bytes;
+    uint64_t budget_bytes;
+} motex_srv_stats;
+
+int motex_srv_create ( motex_server ** srv, int device, uint64_t hbm_budget_bytes, uint32_t max_batch,
+                       uint32_t workers, uint32_t max_queue );
+int motex_srv_submit ( motex_server * srv, const motex_job * job, uint64_t * id );
+int motex_srv_wait ( motex_server * srv, uint64_t id, int timeout_ms, motex_result * out, motex_srv_timing * timing );
+int motex_srv_stats_get ( motex_server * srv, motex_srv_stats * out );
+int motex_srv_destroy ( motex_server * srv );
+
+/*
  * Plain per-pair drop-in for
  *   motifs_extraction_hd/_ed(p, m, t, n, sw, u, v)            (nb_gaps == 0)
  *   structured_motifs_extraction_hd/_ed(p, m, t, n, sw, u, v) (nb_gaps > 0)

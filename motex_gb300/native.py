@@ -24,6 +24,7 @@ EXPORTS = [
     "motex_gpu_load", "motex_gpu_execute", "motex_gpu_fetch", "motex_gpu_extract_pair",
     "motex_gpu_strerror", "motex_gpu_last_error", "motex_ctx_launches", "motex_probe_int_peak",
     "motex_gpu_extract_pair_static", "motex_gpu_run_batch",
+    "motex_srv_create", "motex_srv_submit", "motex_srv_wait", "motex_srv_stats_get", "motex_srv_destroy",
 ]
 
 
@@ -56,6 +57,17 @@ class Result(C.Structure):
                 ("launches", C.c_uint32), ("device_ms", C.c_double), ("dp_ms", C.c_double)]
 
 
+class SrvTiming(C.Structure):
+    _fields_ = [("queue_ms", C.c_double), ("run_ms", C.c_double), ("latency_ms", C.c_double),
+                ("batch_size", C.c_uint32)]
+
+
+class SrvStats(C.Structure):
+    _fields_ = [("submitted", C.c_uint64), ("completed", C.c_uint64), ("failed", C.c_uint64),
+                ("batches", C.c_uint64), ("cells", C.c_uint64), ("max_batch_seen", C.c_uint32),
+                ("queued", C.c_uint32), ("in_use_bytes", C.c_uint64), ("budget_bytes", C.c_uint64)]
+
+
 _lib = None
 
 
@@ -83,6 +95,11 @@ def load_library(path: str = LIB_PATH):
         "motex_ctx_launches": (C.c_uint64, [C.c_void_p]),
         "motex_probe_int_peak": (C.c_int, [C.c_int, P(C.c_double), P(C.c_double), P(C.c_double)]),
         "motex_gpu_run_batch": (C.c_int, [C.c_void_p, P(Job), C.c_uint32, P(Result)]),
+        "motex_srv_create": (C.c_int, [P(C.c_void_p), C.c_int, C.c_uint64, C.c_uint32, C.c_uint32, C.c_uint32]),
+        "motex_srv_submit": (C.c_int, [C.c_void_p, P(Job), P(C.c_uint64)]),
+        "motex_srv_wait": (C.c_int, [C.c_void_p, C.c_uint64, C.c_int, P(Result), P(SrvTiming)]),
+        "motex_srv_stats_get": (C.c_int, [C.c_void_p, P(SrvStats)]),
+        "motex_srv_destroy": (C.c_int, [C.c_void_p]),
         "motex_gpu_extract_pair_static": (C.c_int, [P(Params), C.c_char_p, C.c_void_p, C.c_uint32, C.c_void_p,
                                                     C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p]),
     }
@@ -222,3 +239,46 @@ class Context:
         V = (C.c_uint32 * (m * nb_structs))(*(v or [0] * (m * nb_structs)))
         _check(self.lib.motex_gpu_extract_pair(self.h, C.byref(params), p.encode(), m, t.encode(), len(t), U, V))
         return list(U), list(V)
+
+
+class Server:
+    """Continuous-batching extraction server (motex_srv_*)."""
+
+    def __init__(self, device=0, hbm_budget=0, max_batch=32, workers=2, max_queue=0):
+        self.lib = load_library()
+        self.h = C.c_void_p()
+        _check(self.lib.motex_srv_create(C.byref(self.h), device, hbm_budget, max_batch, workers, max_queue))
+
+    def submit(self, seqs, params: Params) -> int:
+        bs, arr, lens = Context._seq_arrays(seqs)
+        job = Job(C.pointer(params), arr, lens, len(bs))
+        rid = C.c_uint64()
+        _check(self.lib.motex_srv_submit(self.h, C.byref(job), C.byref(rid)))
+        return rid.value
+
+    def wait(self, rid: int, timeout_ms: int = -1):
+        """(Extraction, timing dict); raises MotexError (ETIMEOUT if still pending)."""
+        res, tm = Result(), SrvTiming()
+        rc = self.lib.motex_srv_wait(self.h, rid, timeout_ms, C.byref(res), C.byref(tm))
+        try:
+            _check(rc)
+            return Context._collect(res), {"queue_ms": tm.queue_ms, "run_ms": tm.run_ms,
+                                           "latency_ms": tm.latency_ms, "batch_size": tm.batch_size}
+        finally:
+            self.lib.motex_result_free(C.byref(res))
+
+    def stats(self) -> dict:
+        st = SrvStats()
+        _check(self.lib.motex_srv_stats_get(self.h, C.byref(st)))
+        return {k: getattr(st, k) for k, _ in SrvStats._fields_}
+
+    def close(self):
+        if self.h:
+            self.lib.motex_srv_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()

@@ -89,7 +89,7 @@ def write_boxes(path: str, boxes) -> None:
 
 def _rand_seq(rng, alphabet: str, n: int, p=None) -> str:
     idx = rng.choice(len(alphabet), size=n, p=p)
-    return "".join(np.array(list(alphabet))[idx])
+    return np.frombuffer(alphabet.encode(), dtype=np.uint8)[idx].tobytes().decode()
 
 
 def _substitute(rng, w: str, alphabet: str, nsub: int) -> str:

@@ -20,6 +20,11 @@ first-occurrence compaction) of the workload.
 --impl reference times that CPU implementation alone (the reference's own
 libFLASM build is x86-64 only and its sources are not on the GPU host).
 
+Extra sections of the default line: batched_vs_plain (uneven protein batch,
+whole set in one persistent launch vs one extraction per ordered pair) and
+serving (Poisson request stream through the continuous-batching server vs
+the same arrivals served one request at a time: p50/p99 latency, throughput).
+
 usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--workload NAME] [--impl reference]
 """
 from __future__ import annotations
@@ -190,6 +195,101 @@ def traffic_record(workload):
         return None
 
 
+def dp_kernel_name(wl):
+    if wl.boxes:
+        return "k_dp_struct1"
+    if wl.k > 32:
+        return "k_dp_generic"
+    if wl.d == 1 and 4 <= wl.k <= 15:
+        return f"k_dp_swar_ed (NL={min(4, 33 // (wl.k + 1))})"
+    return "k_dp_fast"
+
+
+def batched_vs_plain(native, ctx, seed=3, sample=30, scale=1.0):
+    """Uneven protein batch (-d 1 -k 10 -e 2 -q 15): the batched persistent
+    form on the whole set against the plain per-pair path (one extraction
+    launch sequence per ordered pair, the reference driver's loop) timed on
+    the ordered pairs of a sample of the sequences."""
+    import time as _t
+    wl = W.prot_uneven(seed=seed, d=1, scale=scale)
+    prm = native.make_params(wl.d, wl.k, wl.e, wl.q)
+    ctx.run_batch([(wl.seqs, prm)])
+    t0 = _t.perf_counter()
+    res = ctx.run_batch([(wl.seqs, prm)])[0]
+    tb = _t.perf_counter() - t0
+    seqs = wl.seqs[:sample]
+    cells = 0
+    ctx.extract_pair(seqs[0], seqs[1], prm)
+    t0 = _t.perf_counter()
+    for x in seqs:
+        for t in seqs:
+            if len(x) >= wl.k and len(t) >= wl.k:
+                ctx.extract_pair(x, t, prm)
+                cells += len(x) * len(t)
+    tp = _t.perf_counter() - t0
+    b, p = res.ref_cells / tb / 1e9, cells / tp / 1e9
+    return {"workload": "prot_uneven_d1", "batched_gcups": round(b, 1), "batched_ms": round(tb * 1e3, 2),
+            "plain_gcups": round(p, 3), "plain_pairs": len(seqs) ** 2, "ratio": round(b / p, 1),
+            "note": "batched: whole set, one persistent DP launch; plain: motex_gpu_extract_pair per ordered pair "
+                    f"of the first {sample} sequences (host wall time, both)"}
+
+
+def serving(native, nreq=300, rate_hz=100.0, seed=5, max_batch=32, workers=2):
+    """Poisson request stream through the continuous-batching server, and
+    the same arrivals served one request at a time (plain per-request GPU
+    path, FIFO).  Latency = completion - arrival."""
+    import threading
+    import time as _t
+    stream = W.serve_stream(seed=seed, nreq=nreq, rate_hz=rate_hz)
+    reqs = [(t, wl.seqs, native.make_params(wl.d, wl.k, wl.e, wl.q)) for t, wl in stream]
+    cells = [sum(map(len, s)) ** 2 for _, s, _ in reqs]
+
+    def pct(xs, q):
+        xs = sorted(xs)
+        return xs[min(len(xs) - 1, int(round(q / 100 * (len(xs) - 1))))]
+
+    out = {"requests": nreq, "rate_hz": rate_hz, "max_batch": max_batch, "workers": workers}
+    with native.Server(max_batch=max_batch, workers=workers) as srv:
+        ids = [None] * nreq
+        lat = [None] * nreq
+        t0 = _t.perf_counter()
+
+        def submitter():
+            for i, (t, s, p) in enumerate(reqs):
+                d = t0 + t - _t.perf_counter()
+                if d > 0:
+                    _t.sleep(d)
+                ids[i] = srv.submit(s, p)
+
+        th = threading.Thread(target=submitter)
+        th.start()
+        for i in range(nreq):
+            while ids[i] is None:
+                _t.sleep(0.0005)
+            _, tm = srv.wait(ids[i])
+            lat[i] = tm["latency_ms"]
+        th.join()
+        wall = _t.perf_counter() - t0
+        st = srv.stats()
+    out["batched"] = {"p50_ms": round(pct(lat, 50), 2), "p99_ms": round(pct(lat, 99), 2),
+                      "req_per_s": round(nreq / wall, 1), "gcups": round(sum(cells) / wall / 1e9, 1),
+                      "batches": st["batches"], "max_batch_seen": st["max_batch_seen"]}
+    ctx = native.Context(0)
+    lat2 = []
+    t0 = _t.perf_counter()
+    for t, s, p in reqs:
+        d = t0 + t - _t.perf_counter()
+        if d > 0:
+            _t.sleep(d)
+        ctx.run(s, p)
+        lat2.append((_t.perf_counter() - t0 - t) * 1e3)
+    wall2 = _t.perf_counter() - t0
+    ctx.close()
+    out["plain"] = {"p50_ms": round(pct(lat2, 50), 2), "p99_ms": round(pct(lat2, 99), 2),
+                    "req_per_s": round(nreq / wall2, 1), "gcups": round(sum(cells) / wall2 / 1e9, 1)}
+    return out
+
+
 def run_gpu(args, rank, world, local_rank):
     import ctypes as C
     import torch
@@ -278,13 +378,19 @@ def run_gpu(args, rank, world, local_rank):
     dp_s = statistics.mean(dp_ms) / 1e3
     achieved = alg_ops / dp_s / 1e12 if dp_s > 0 else 0.0
     tr = traffic_record(args.workload)
-    roofline = {"bound": "int32_alu", "kernel": "k_dp_fast", "achieved": round(achieved, 3),
-                "peak": round(lop3, 3), "unit": "Tops/s", "frac": round(achieved / lop3, 4) if lop3 else None,
-                "peak_source": "measured lop3 throughput probe (motex_probe_int_peak), same run",
-                "iadd_peak": round(iadd, 3), "popc_peak": round(popc, 3),
+    kernel = dp_kernel_name(wl)
+    roofline = {"bound": "int32_alu", "kernel": kernel, "achieved": round(achieved, 3),
+                "peak": round(iadd, 3), "unit": "Tops/s", "frac": round(achieved / iadd, 4) if iadd else None,
+                "peak_source": "measured int32 add throughput, all pipes (motex_probe_int_peak), same run",
+                "lop3_pipe_peak": round(lop3, 3), "popc_peak": round(popc, 3),
                 "ops_per_cell": OPS_PER_CELL[wl.d], "cells_per_launch": first.unique_words * total_pos,
-                "dp_ms": round(dp_s * 1e3, 3), "traffic": tr}
+                "dp_ms": round(dp_s * 1e3, 3), "dp_cells_per_s": round(first.unique_words * total_pos / dp_s, 1),
+                "traffic": tr}
 
+    extras = {}
+    if rank == 0 and not args.no_extras and args.scale == 1.0:
+        extras["batched_vs_plain"] = batched_vs_plain(native, ctx)
+        extras["serving"] = serving(native)
     out = {
         "metric": "GCUPS (reference DP cell updates per second), whole-set word-based motif extraction",
         "value": round(value, 2), "unit": "GCUPS", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
@@ -302,6 +408,7 @@ def run_gpu(args, rank, world, local_rank):
         "clocks": clocks,
         "measured_peaks": {k: measured_peaks().get(k) for k in ("hbm_gbs", "bf16_tflops")},
     }
+    out.update(extras)
     ctx.close()
     return out, wl
 
@@ -342,6 +449,8 @@ def main():
     ap.add_argument("--scale", type=float, default=1.0,
                     help="shrink the workload (profiling captures only; 1.0 = the benchmark size)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the batched-vs-plain and serving sections")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
     rank = int(os.environ.get("RANK", "0"))

@@ -282,3 +282,271 @@ __global__ void k_struct_finalize ( StructFinalizeArgs a )
 }
 
 } // namespace mtx
+
+// ===================================================================== N gaps
+//
+// Structured motifs with any number of gaps (functions.cc:647-690 merge loop).
+// One thread per pattern position jx runs the box-0 DP over the text chunk.
+// On a box-0 hit at text position it, it enumerates every pattern structure
+// k and text structure l like the reference's merge: box g+1 of the pattern
+// ends at jx + xoff[k][g], the text box at it + xoff[l][g] (cumulative gap +
+// box lengths), and both must lie inside their sequences.  Later boxes are
+// checked directly at that end position: Hamming compares one window of the
+// text bit planes with the box factor's planes; edit distance reruns the
+// Myers column over the last l_b + e_b text symbols (a restart that far back
+// is exact for the <= e_b test) or from the sequence start.
+
+namespace mtx
+{
+
+namespace
+{
+
+template <int B>
+__device__ __forceinline__ void text_window ( const TextView & tv, uint32_t p, uint32_t ( &Y )[B] )
+{
+    // 32 symbols ending at p (p at bit 31)
+    const uint32_t blk = p >> 5, r = p & 31u;
+#pragma unroll
+    for ( int b = 0; b < B; ++b )
+    {
+        const uint32_t lo = __ldg ( tv.planes + ( size_t ) b * tv.plane_stride + blk );
+        const uint32_t hi = __ldg ( tv.planes + ( size_t ) b * tv.plane_stride + blk + 1 );
+        Y[b] = __funnelshift_rc ( lo, hi, r + 1 );
+    }
+}
+
+template <int B, bool ED>
+__device__ bool box_hit ( const StructNArgs & a, int box, uint32_t q, uint32_t p, uint32_t tstart )
+{
+    const uint32_t lb = a.blen[box], eb = a.berr[box];
+    const uint32_t * __restrict__ wpl = a.wpl + ( size_t ) box * B * a.total;
+    uint32_t w[B];
+#pragma unroll
+    for ( int b = 0; b < B; ++b ) w[b] = __ldg ( wpl + ( size_t ) b * a.total + q );
+    if constexpr ( ! ED )
+    {
+        uint32_t Y[B];
+        text_window<B> ( a.text, p, Y );
+        const uint32_t top = lb >= 32 ? 0xffffffffu : ~( ( 1u << ( 32 - lb ) ) - 1u );
+        uint32_t x = w[0] ^ Y[0];
+#pragma unroll
+        for ( int b = 1; b < B; ++b ) x |= w[b] ^ Y[b];
+        return __popc ( x & top ) <= eb;
+    }
+    else
+    {
+        const uint32_t back = lb + eb - 1;
+        const uint32_t s0 = ( p >= tstart + back ) ? p - back : tstart;
+        uint32_t Pv = ~0u, Mv = 0, sc = lb;
+        const uint32_t sh = lb - 1;
+        for ( uint32_t r = s0; r <= p; ++r )
+        {
+            const uint32_t blk = ( r >> 5 ) + 1, bit = r & 31u;
+            uint32_t x = 0;
+#pragma unroll
+            for ( int b = 0; b < B; ++b )
+            {
+                const uint32_t T = 0u - ( ( __ldg ( a.text.planes + ( size_t ) b * a.text.plane_stride + blk ) >> bit ) & 1u );
+                x |= w[b] ^ T;
+            }
+            const uint32_t Eq = ~x;
+            const uint32_t Xv = Eq | Mv;
+            const uint32_t Xh = ( ( ( Eq & Pv ) + Pv ) ^ Pv ) | Eq;
+            uint32_t Ph = Mv | ~( Xh | Pv );
+            uint32_t Mh = Pv & Xh;
+            sc += ( ( Ph >> sh ) & 1u ) - ( ( Mh >> sh ) & 1u );
+            Ph <<= 1;
+            Mh <<= 1;
+            Pv = Mh | ~( Xv | Ph );
+            Mv = Ph & Xv;
+        }
+        return sc <= eb;
+    }
+}
+
+} // namespace
+
+template <int B, bool ED>
+__global__ void __launch_bounds__ ( kDPThreads ) k_dp_structN ( const StructNArgs a )
+{
+    extern __shared__ uint32_t smem[];
+    const uint32_t NS = a.nstructs, NG = a.ngaps;
+    uint32_t * s_off = smem;                                        // NS * NG cumulative offsets
+    uint32_t * s_cnt = smem + NS * NG + threadIdx.x;                // [k * kDPThreads + tid]
+    uint32_t * s_u = s_cnt + NS * kDPThreads;
+    uint32_t * s_v = s_u + NS * kDPThreads;
+    for ( uint32_t i = threadIdx.x; i < NS * NG; i += kDPThreads ) s_off[i] = a.xoff[i];
+    for ( uint32_t k = 0; k < NS; ++k ) s_cnt[k * kDPThreads] = s_u[k * kDPThreads] = s_v[k * kDPThreads] = 0;
+    __syncthreads ();
+
+    const uint32_t jx = blockIdx.x * kDPThreads + threadIdx.x;
+    const bool row = jx < a.total && a.row_ok[jx];
+    const uint32_t xend = jx < a.total ? a.row_end[jx] : 0;
+    uint32_t w0[B];
+#pragma unroll
+    for ( int b = 0; b < B; ++b ) w0[b] = jx < a.total ? a.wpl[( size_t ) b * a.total + jx] : 0u;
+    const uint32_t l0 = a.l0;
+    const uint32_t top0 = l0 >= 32 ? 0xffffffffu : ~( ( 1u << ( 32 - l0 ) ) - 1u );
+    const ChunkInfo ch = a.chunks[blockIdx.y];
+    int cur_split = ch.first_split;
+    uint32_t Pv = ~0u, Mv = 0, sc = l0;
+    uint32_t tstart = 0;                                            // start of the current text sequence
+    bool tstart_known = false;
+    uint32_t prev[B];
+#pragma unroll
+    for ( int b = 0; b < B; ++b ) prev[b] = __ldg ( a.text.planes + ( size_t ) b * a.text.plane_stride + ch.warm );
+
+    auto flush = [&] () {
+        for ( uint32_t k = 0; k < NS; ++k )
+        {
+            const uint32_t c = s_cnt[k * kDPThreads];
+            if ( ! c ) continue;
+            if ( cur_split < 0 ) s_u[k * kDPThreads] += 1;
+            else if ( jx < a.total ) a.split_flags[( ( size_t ) cur_split * a.total + jx ) * NS + k] = 1;
+            s_v[k * kDPThreads] += c;
+            s_cnt[k * kDPThreads] = 0;
+        }
+    };
+
+    for ( uint32_t kb = ch.warm; kb < ch.end; ++kb )
+    {
+        uint32_t cur[B];
+#pragma unroll
+        for ( int b = 0; b < B; ++b ) cur[b] = __ldg ( a.text.planes + ( size_t ) b * a.text.plane_stride + kb + 1 );
+        const uint32_t vm = __ldg ( a.text.vmask + kb ), em = __ldg ( a.text.emask + kb );
+        const bool counting = kb >= ch.begin;
+        for ( int r = 0; r < 32; ++r )
+        {
+            const uint32_t it = kb * 32 + r;
+            bool h0;
+            if constexpr ( ED )
+            {
+                uint32_t x = 0;
+#pragma unroll
+                for ( int b = 0; b < B; ++b ) x |= w0[b] ^ ( 0u - ( ( cur[b] >> r ) & 1u ) );
+                const uint32_t Eq = ~x;
+                const uint32_t Xv = Eq | Mv;
+                const uint32_t Xh = ( ( ( Eq & Pv ) + Pv ) ^ Pv ) | Eq;
+                uint32_t Ph = Mv | ~( Xh | Pv );
+                uint32_t Mh = Pv & Xh;
+                sc += ( ( Ph >> ( l0 - 1 ) ) & 1u ) - ( ( Mh >> ( l0 - 1 ) ) & 1u );
+                Ph <<= 1;
+                Mh <<= 1;
+                Pv = Mh | ~( Xv | Ph );
+                Mv = Ph & Xv;
+                h0 = sc <= a.e0;
+            }
+            else
+            {
+                uint32_t x = 0;
+#pragma unroll
+                for ( int b = 0; b < B; ++b ) x |= w0[b] ^ __funnelshift_rc ( prev[b], cur[b], r + 1 );
+                h0 = __popc ( x & top0 ) <= a.e0;
+            }
+            if ( row && counting && h0 && ( ( vm >> r ) & 1u ) )
+            {
+                if ( ! tstart_known )
+                {
+                    tstart = a.seq_start[it];                   // once per text sequence and chunk
+                    tstart_known = true;
+                }
+                const uint32_t tend = a.row_end[it];
+                for ( uint32_t k = 0; k < NS; ++k )
+                {
+                    if ( jx + s_off[k * NG + NG - 1] >= xend ) continue;      // x structure must fit
+                    for ( uint32_t l = 0; l < NS; ++l )
+                    {
+                        bool ok = true;
+                        for ( uint32_t g = 0; g < NG && ok; ++g )
+                        {
+                            const uint32_t q = jx + s_off[k * NG + g], p = it + s_off[l * NG + g];
+                            ok = p < tend && box_hit<B, ED> ( a, ( int ) g + 1, q, p, tstart );
+                        }
+                        if ( ok ) s_cnt[k * kDPThreads] += 1;
+                    }
+                }
+            }
+            if ( ( em >> r ) & 1u )
+            {
+                if ( counting )
+                {
+                    flush ();
+                    cur_split = -1;
+                }
+                Pv = ~0u;
+                Mv = 0;
+                sc = l0;
+                tstart_known = false;
+            }
+        }
+#pragma unroll
+        for ( int b = 0; b < B; ++b ) prev[b] = cur[b];
+    }
+    for ( uint32_t k = 0; k < NS; ++k )
+    {
+        const uint32_t c = s_cnt[k * kDPThreads];
+        uint32_t u = s_u[k * kDPThreads];
+        if ( c )
+        {
+            if ( ch.last_split >= 0 && jx < a.total )
+                a.split_flags[( ( size_t ) ch.last_split * a.total + jx ) * NS + k] = 1;
+            else
+                u += 1;
+        }
+        const uint32_t v = s_v[k * kDPThreads] + c;
+        if ( jx < a.total && ( u | v ) )
+        {
+            atomicAdd ( a.u_acc + ( size_t ) jx * NS + k, u );
+            atomicAdd ( a.v_acc + ( size_t ) jx * NS + k, v );
+        }
+    }
+}
+
+bool launch_dp_structN ( const StructNArgs & a, int B, bool ed, dim3 grid, cudaStream_t st )
+{
+    if ( a.l0 < 1 || a.l0 > 32 || a.nstructs < 1 || a.nstructs > kMaxStructsN || a.ngaps < 1 || a.ngaps > kMaxGapsN )
+        return false;
+    for ( uint32_t g = 0; g <= a.ngaps; ++g )
+        if ( a.blen[g] < 1 || a.blen[g] > 32 ) return false;
+    const size_t smem = ( ( size_t ) a.nstructs * a.ngaps + ( size_t ) 3 * a.nstructs * kDPThreads ) * sizeof ( uint32_t );
+#define MTX_SN( BB )                                                                                   \
+    case BB:                                                                                           \
+        if ( ed )                                                                                      \
+        {                                                                                              \
+            cudaFuncSetAttribute ( k_dp_structN<BB, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, ( int ) smem ); \
+            k_dp_structN<BB, true><<<grid, kDPThreads, smem, st>>> ( a );                              \
+        }                                                                                              \
+        else                                                                                           \
+        {                                                                                              \
+            cudaFuncSetAttribute ( k_dp_structN<BB, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, ( int ) smem ); \
+            k_dp_structN<BB, false><<<grid, kDPThreads, smem, st>>> ( a );                             \
+        }                                                                                              \
+        return true;
+    switch ( B )
+    {
+        MTX_SN ( 2 )
+        MTX_SN ( 3 )
+        MTX_SN ( 4 )
+        MTX_SN ( 5 )
+        default: return false;
+    }
+#undef MTX_SN
+}
+
+// Start offset of the sequence holding each position.
+__global__ void k_seq_start ( const uint32_t * __restrict__ offs, uint32_t nseq, uint64_t total, uint32_t * out )
+{
+    const uint32_t pos = blockIdx.x * blockDim.x + threadIdx.x;
+    if ( pos >= total ) return;
+    uint32_t lo = 0, hi = nseq;
+    while ( hi - lo > 1 )
+    {
+        const uint32_t mid = ( lo + hi ) >> 1;
+        if ( offs[mid] <= pos ) lo = mid; else hi = mid;
+    }
+    while ( offs[lo + 1] <= pos ) ++lo;
+    out[pos] = offs[lo];
+}
+
+} // namespace mtx

@@ -110,6 +110,30 @@ struct StructFinalizeArgs
 };
 
 bool launch_dp_struct1 ( const StructArgs & a, int B, bool ed, dim3 grid, cudaStream_t st );
+
+// Structured motifs with any number of gaps (dp_struct.cu, k_dp_structN).
+constexpr uint32_t kMaxStructsN = 32;
+constexpr uint32_t kMaxGapsN = 8;
+struct StructNArgs
+{
+    TextView          text;
+    const uint32_t *  wpl;           // box b's planes at [(b * B + plane) * total + pos]
+    const uint8_t *   row_ok;
+    const uint32_t *  row_end;       // end offset of the position's sequence
+    const uint32_t *  seq_start;     // start offset of the position's sequence
+    const uint32_t *  xoff;          // [k * ngaps + g]: end of box g+1 minus end of box 0, structure k
+    uint32_t          total;
+    uint32_t          l0, e0;
+    uint32_t          blen[kMaxGapsN + 1];   // box lengths, blen[0] = l0
+    uint32_t          berr[kMaxGapsN + 1];
+    uint32_t          ngaps, nstructs;
+    const ChunkInfo * chunks;
+    uint32_t *        u_acc;         // [pos * nstructs + k]
+    uint32_t *        v_acc;
+    uint8_t *         split_flags;   // n_split rows of total * nstructs bytes
+};
+bool launch_dp_structN ( const StructNArgs & a, int B, bool ed, dim3 grid, cudaStream_t st );
+__global__ void k_seq_start ( const uint32_t * offs, uint32_t nseq, uint64_t total, uint32_t * out );
 __global__ void k_wplanes_all ( const uint8_t * codes, uint32_t total, uint32_t l, uint32_t B, int top_aligned,
                                 uint32_t * out );
 __global__ void k_struct_rows ( const uint32_t * offs, uint32_t nseq, uint64_t total, uint32_t l0, uint32_t tml,

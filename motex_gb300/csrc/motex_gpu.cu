@@ -23,6 +23,7 @@
 #include <cstring>
 #include <map>
 #include <memory>
+#include <mutex>
 #include <string>
 #include <tuple>
 #include <unordered_set>
@@ -71,13 +72,14 @@ enum Slot
     S_RAW, S_OFFS, S_WSTART, S_QOK, S_CMAP, S_PRESENT, S_CODES, S_PLANES, S_VMASK, S_EMASK,
     S_WPOS, S_KEY0, S_KEY1, S_IDX1, S_HIST, S_HEAD, S_PREF, S_UNIQ, S_WPL32, S_WPL64,
     S_CHUNKS, S_UACC, S_VACC, S_FLAGS, S_MARK, S_RECU, S_RECV, S_PREF2, S_RECS, S_TILES,
-    S_SCALAR, S_UOUT, S_VOUT, S_WPL0, S_WPL1, S_ROWOK, S_ROWEND, S_COUNT
+    S_SCALAR, S_UOUT, S_VOUT, S_WPL0, S_WPL1, S_ROWOK, S_ROWEND, S_WPLN, S_SEQSTART, S_XOFF, S_COUNT
 };
 
 // Pinned staging layout of a job (bytes).
 constexpr size_t kPinPresent = 0;          // 256 x u32 symbol presence
 constexpr size_t kPinCmap = 1024;          // 256 B symbol -> code
 constexpr size_t kPinScalar = 2048;        // u32 unique count, u32 motif count
+constexpr size_t kPinXoff = 2560;          // structure offset table (<= 384 u32)
 constexpr size_t kPinChunks = 4096;        // chunk table
 constexpr size_t kPinStage = 65536;        // input upload / result download
 constexpr uint32_t kMaxChunks = ( kPinStage - kPinChunks ) / sizeof ( ChunkInfo );
@@ -123,9 +125,12 @@ struct Job
 
     // plan of the DP launch
     bool structured = false, generic = false, dp_pending = false, dp_timed = false, replaying = false;
+    bool batched = false;                      // a member of a batch (persistent DP launch)
     uint32_t nw64 = 1;
     DPArgs da {};
     StructArgs sa {};
+    StructNArgs san {};
+    bool structN = false;
     std::vector<ChunkInfo> chunks;
     uint32_t ntiles = 0;
     uint32_t * uniq = nullptr;
@@ -245,6 +250,15 @@ int check_launch ( Job * j, const char * what )
 
 unsigned blocks_for ( uint64_t n, unsigned threads ) { return ( unsigned ) std::max<uint64_t> ( 1, ( n + threads - 1 ) / threads ); }
 
+// Timing event on the job's stream; while a graph is being captured it is
+// recorded as an external node, so the replayed graph records it too.
+int record ( Job * j, cudaEvent_t ev )
+{
+    if ( j->replaying ) MTX_CUDA ( cudaEventRecordWithFlags ( ev, j->ctx->st, cudaEventRecordExternal ) );
+    else MTX_CUDA ( cudaEventRecord ( ev, j->ctx->st ) );
+    return MOTEX_OK;
+}
+
 int init_job ( motex_ctx * c, Job * j )
 {
     j->ctx = c;
@@ -264,6 +278,14 @@ void drop_graph ( Job * j )
     j->runs_since_load = 0;
 }
 
+// One gap within the shared-history kernel's limits (k_dp_struct1).
+bool struct1_shape ( const motex_params * p )
+{
+    if ( p->nb_gaps != 1 ) return false;
+    const uint32_t gmin = p->gap_min[0], gmax = p->gap_max[0], b1 = p->blens[0];
+    return p->l <= 32 && b1 <= 32 && gmax >= gmin && gmax - gmin + 1 <= 32 && gmax + b1 <= 31;
+}
+
 int validate ( const motex_params * p )
 {
     if ( ! p ) return fail ( MOTEX_EINVAL, "null parameters" );
@@ -274,15 +296,25 @@ int validate ( const motex_params * p )
     if ( p->nb_gaps )
     {
         if ( ! p->gap_min || ! p->gap_max || ! p->blens || ! p->berrs ) return fail ( MOTEX_EINVAL, "null box arrays" );
-        if ( p->nb_gaps > 1 )
-            return fail ( MOTEX_EUNSUPPORTED, "structured motifs with %u gaps (one gap is implemented)", p->nb_gaps );
-        const uint32_t gmin = p->gap_min[0], gmax = p->gap_max[0], b1 = p->blens[0];
-        if ( gmax < gmin ) return fail ( MOTEX_EINVAL, "gap range [%u,%u] is empty", gmin, gmax );
-        if ( b1 == 0 ) return fail ( MOTEX_EINVAL, "box length must be positive" );
-        if ( p->l > 32 || b1 > 32 || gmax - gmin + 1 > 32 || gmax + b1 > 31 )
-            return fail ( MOTEX_EUNSUPPORTED, "structured boxes need l, box length <= 32, gap max + box length <= 31 and at most 32 gap choices" );
-        if ( p->berrs[0] >= p->l + gmin + b1 )
-            return fail ( MOTEX_EUNSUPPORTED, "box error bound %u not below the minimum motif length", p->berrs[0] );
+        if ( p->nb_gaps > kMaxGapsN )
+            return fail ( MOTEX_EUNSUPPORTED, "structured motifs with %u gaps (at most %u)", p->nb_gaps, kMaxGapsN );
+        if ( p->l > 32 ) return fail ( MOTEX_EUNSUPPORTED, "structured motifs need l <= 32" );
+        uint64_t structs = 1, tml = p->l;
+        for ( uint32_t g = 0; g < p->nb_gaps; ++g )
+        {
+            if ( p->gap_max[g] < p->gap_min[g] ) return fail ( MOTEX_EINVAL, "gap range [%u,%u] is empty", p->gap_min[g], p->gap_max[g] );
+            if ( p->blens[g] == 0 ) return fail ( MOTEX_EINVAL, "box length must be positive" );
+            if ( p->blens[g] > 32 ) return fail ( MOTEX_EUNSUPPORTED, "structured boxes need box length <= 32" );
+            structs *= p->gap_max[g] - p->gap_min[g] + 1;
+            if ( structs > 1u << 20 ) break;
+            tml += p->gap_min[g] + p->blens[g];
+        }
+        if ( ! struct1_shape ( p ) && structs > kMaxStructsN )
+            return fail ( MOTEX_EUNSUPPORTED, "%llu gap structures (at most %u with several gaps or long gaps)",
+                          ( unsigned long long ) structs, kMaxStructsN );
+        for ( uint32_t g = 0; g < p->nb_gaps; ++g )
+            if ( p->berrs[g] >= tml )
+                return fail ( MOTEX_EUNSUPPORTED, "box error bound %u not below the minimum motif length", p->berrs[g] );
     }
     return MOTEX_OK;
 }
@@ -358,6 +390,124 @@ DPTune choose_tune ( Job * j, uint32_t U, bool ed, bool generic )
 }
 
 /*
+ * Autotuner.  For a job with at least kTuneMinCells DP cells whose key
+ * (bit planes B, factor length l, errors e, distance d) has no entry yet,
+ * every candidate launch shape -- register words per thread W, factors per
+ * register NL (SWAR or 1-lane for edit distance), block unroll UR -- runs the
+ * DP on a probe: one full wave of tiles (at most 8 per SM) over a 512-block
+ * text chunk, long enough that the per-CTA set-up weighs as little as in the
+ * real run; time per cell from CUDA events picks the winner, accumulators
+ * are cleared afterwards.  Batched jobs are not tuned (the persistent kernels
+ * have a fixed shape).  Entries are shared by every context of the
+ * process and, with MOTEX_TUNE_CACHE=<file>, read from and appended to that
+ * file.  MOTEX_AUTOTUNE=0 turns tuning off (the defaults of choose_tune
+ * apply); explicit MOTEX_DP_* overrides win over both.
+ */
+constexpr uint64_t kTuneMinCells = 50000000000ull;
+constexpr uint32_t kTuneBlocks = 512;        // probe chunk: 16384 text positions
+
+struct TuneKey
+{
+    int B;
+    uint32_t l, e, d;
+    bool operator< ( const TuneKey & o ) const { return std::tie ( B, l, e, d ) < std::tie ( o.B, o.l, o.e, o.d ); }
+};
+
+std::mutex g_tune_mu;
+std::map<TuneKey, DPTune> g_tune;
+bool g_tune_loaded = false;
+
+void tune_load_locked ()
+{
+    if ( g_tune_loaded ) return;
+    g_tune_loaded = true;
+    const char * path = getenv ( "MOTEX_TUNE_CACHE" );
+    if ( ! path || ! *path ) return;
+    FILE * f = fopen ( path, "r" );
+    if ( ! f ) return;
+    TuneKey k;
+    DPTune t;
+    while ( fscanf ( f, "%d %u %u %u %d %d %d", &k.B, &k.l, &k.e, &k.d, &t.W, &t.NL, &t.UR ) == 7 ) g_tune[k] = t;
+    fclose ( f );
+}
+
+void tune_store_locked ( const TuneKey & k, const DPTune & t )
+{
+    g_tune[k] = t;
+    const char * path = getenv ( "MOTEX_TUNE_CACHE" );
+    if ( ! path || ! *path ) return;
+    if ( FILE * f = fopen ( path, "a" ) )
+    {
+        fprintf ( f, "%d %u %u %u %d %d %d\n", k.B, k.l, k.e, k.d, t.W, t.NL, t.UR );
+        fclose ( f );
+    }
+}
+
+bool tune_lookup ( const TuneKey & k, DPTune * t )
+{
+    std::lock_guard<std::mutex> lk ( g_tune_mu );
+    tune_load_locked ();
+    auto it = g_tune.find ( k );
+    if ( it == g_tune.end () ) return false;
+    *t = it->second;
+    return true;
+}
+
+bool launch_shape ( Job * j, const DPArgs & da, const DPTune & t, dim3 grid )
+{
+    const bool ed = j->prm.d == 1;
+    return t.NL > 1 ? launch_dp_swar_ed ( da, j->B, t.NL, t.W, t.UR, grid, j->ctx->st )
+                    : launch_dp_fast ( da, j->B, t.W, t.UR, ed, grid, j->ctx->st );
+}
+
+int autotune ( Job * j, DPTune * best )
+{
+    const bool ed = j->prm.d == 1;
+    const TuneKey key { j->B, j->prm.l, j->prm.e, j->prm.d };
+    std::vector<DPTune> cands;
+    for ( int NL : { swar_lanes ( j->prm.l ), 1 } )
+    {
+        if ( ! ed && NL > 1 ) continue;
+        for ( int W : { 4, 8 } )
+            for ( int UR : { 4, 8 } )
+                cands.push_back ( DPTune { W, NL, UR } );
+        if ( NL == 1 ) break;
+    }
+    // probe chunk: 64 blocks from the start of the text, no splits
+    ChunkInfo probe { 0, 0, std::min<uint32_t> ( j->nblk, kTuneBlocks ), -1, -1 };
+    ChunkInfo * d_probe;
+    MTX_TRY ( ensure ( j, S_TILES, ( sizeof ( ChunkInfo ) + 3 ) / 4, reinterpret_cast<uint32_t **> ( &d_probe ) ) );
+    ChunkInfo * h_probe = pin<ChunkInfo> ( j, kPinChunks );
+    *h_probe = probe;
+    MTX_CUDA ( cudaMemcpyAsync ( d_probe, h_probe, sizeof probe, cudaMemcpyHostToDevice, j->ctx->st ) );
+    DPArgs da = j->da;
+    da.chunks = d_probe;
+    float best_ms = 1e30f;
+    for ( const DPTune & t : cands )
+    {
+        const uint32_t groups = ( j->U + t.NL - 1 ) / t.NL;
+        const uint32_t ntiles = ( groups + kDPThreads * t.W - 1 ) / ( kDPThreads * t.W );
+        const dim3 grid ( std::min<uint32_t> ( ntiles, 8u * j->ctx->num_sms ), 1 );
+        for ( int rep = 0; rep < 2; ++rep )                     // first launch warms up
+        {
+            MTX_TRY ( record ( j, j->evd0 ) );
+            if ( ! launch_shape ( j, da, t, grid ) ) return fail ( MOTEX_EUNSUPPORTED, "autotune candidate failed" );
+            MTX_TRY ( check_launch ( j, "k_dp (autotune)" ) );
+            MTX_TRY ( record ( j, j->evd1 ) );
+        }
+        MTX_CUDA ( cudaEventSynchronize ( j->evd1 ) );
+        float ms = 0.f;
+        MTX_CUDA ( cudaEventElapsedTime ( &ms, j->evd0, j->evd1 ) );
+        // normalise by the factors the probe covered
+        const double per = ms / ( double ) std::min<uint64_t> ( ( uint64_t ) grid.x * kDPThreads * t.W * t.NL, j->U );
+        if ( per < best_ms ) { best_ms = ( float ) per; *best = t; }
+    }
+    std::lock_guard<std::mutex> lk ( g_tune_mu );
+    tune_store_locked ( key, *best );
+    return MOTEX_OK;
+}
+
+/*
  * Text chunks for the DP grid: equal block ranges; sequences cut by a chunk
  * boundary get a split index (one flag row each).  warmup = positions a
  * chunk must process before its first counted one (edit distance: l+e-1,
@@ -418,14 +568,6 @@ int upload_chunks ( Job * j, ChunkInfo ** d_out )
 
 // ---------------------------------------------------------------- stages
 
-// Timing event on the job's stream; while a graph is being captured it is
-// recorded as an external node, so the replayed graph records it too.
-int record ( Job * j, cudaEvent_t ev )
-{
-    if ( j->replaying ) MTX_CUDA ( cudaEventRecordWithFlags ( ev, j->ctx->st, cudaEventRecordExternal ) );
-    else MTX_CUDA ( cudaEventRecord ( ev, j->ctx->st ) );
-    return MOTEX_OK;
-}
 
 int stage_presence ( Job * j )
 {
@@ -563,6 +705,16 @@ int stage_plan ( Job * j, bool sorted )
     da.l = P.l;
     da.e = P.e;
     if ( ! j->replaying ) j->tune = choose_tune ( j, U, ed, j->generic );
+    bool tune_now = false;
+    if ( ! j->replaying && ! j->generic && ! j->batched && ! getenv ( "MOTEX_DP_W" ) && ! getenv ( "MOTEX_DP_UR" ) &&
+         ! getenv ( "MOTEX_DP_SWAR" ) )
+    {
+        const char * at = getenv ( "MOTEX_AUTOTUNE" );
+        const bool enabled = ! ( at && atoi ( at ) == 0 );
+        DPTune cached;
+        if ( enabled && tune_lookup ( TuneKey { B, P.l, P.e, P.d }, &cached ) ) j->tune = cached;
+        else tune_now = enabled && ( uint64_t ) U * j->total >= kTuneMinCells;
+    }
     const DPTune & tune = j->tune;
     const uint32_t groups = ( U + tune.NL - 1 ) / tune.NL;        // factors per register: NL
     const uint32_t per_cta = ( uint32_t ) kDPThreads * tune.W;
@@ -589,6 +741,22 @@ int stage_plan ( Job * j, bool sorted )
     uint32_t nchunks = std::max<uint32_t> ( 1, ( target + j->ntiles - 1 ) / j->ntiles );
     const uint32_t min_blocks = ed ? 16 : 4;
     nchunks = std::min<uint32_t> ( nchunks, std::max<uint32_t> ( 1, ( j->nblk - first_blk ) / min_blocks ) );
+    if ( tune_now )
+    {
+        // the probe runs before the real chunk table and the accumulator clears
+        da.u_acc = u_acc;
+        da.v_acc = v_acc;
+        uint8_t * fl;
+        MTX_TRY ( ensure ( j, S_FLAGS, U, &fl ) );
+        da.split_flags = fl;
+        DPTune best = j->tune;
+        MTX_TRY ( autotune ( j, &best ) );
+        j->tune = best;
+        const uint32_t g2 = ( U + best.NL - 1 ) / best.NL;
+        j->ntiles = ( g2 + kDPThreads * best.W - 1 ) / ( kDPThreads * best.W );
+        nchunks = std::max<uint32_t> ( 1, ( target + j->ntiles - 1 ) / j->ntiles );
+        nchunks = std::min<uint32_t> ( nchunks, std::max<uint32_t> ( 1, ( j->nblk - first_blk ) / min_blocks ) );
+    }
     build_chunks ( j, first_blk, nchunks, warmup, j->chunks );
     ChunkInfo * d_chunks;
     MTX_TRY ( upload_chunks ( j, &d_chunks ) );
@@ -613,9 +781,13 @@ int stage_plan ( Job * j, bool sorted )
  * u and v are computed per pattern position like the reference, and the
  * key deduplication of the writer happens on the passing entries only.
  */
+int plan_structured_n ( Job * j );
+
 int plan_structured ( Job * j )
 {
     const motex_params & P = j->prm;
+    if ( ! struct1_shape ( &P ) ) return plan_structured_n ( j );
+    j->structN = false;
     const bool ed = P.d == 1;
     cudaStream_t st = j->ctx->st;
     const int B = j->B;
@@ -685,6 +857,107 @@ int plan_structured ( Job * j )
     return MOTEX_OK;
 }
 
+/*
+ * Structured motifs with several gaps (or one gap outside the shared-history
+ * kernel's limits): the box-0 DP per pattern position with a direct check
+ * of the later boxes at every box-0 hit (k_dp_structN).
+ */
+int plan_structured_n ( Job * j )
+{
+    const motex_params & P = j->prm;
+    const bool ed = P.d == 1;
+    cudaStream_t st = j->ctx->st;
+    const int B = j->B;
+    const uint32_t T = ( uint32_t ) j->total, NS = j->G, NG = P.nb_gaps;
+    j->structN = true;
+    const uint8_t * codes = dptr<uint8_t> ( j, S_CODES );
+    uint32_t *wpl, *row_end, *seq_start, *xoff;
+    uint8_t * row_ok;
+    MTX_TRY ( ensure ( j, S_WPLN, ( size_t ) ( NG + 1 ) * B * T, &wpl ) );
+    MTX_TRY ( ensure ( j, S_ROWOK, T, &row_ok ) );
+    MTX_TRY ( ensure ( j, S_ROWEND, T, &row_end ) );
+    MTX_TRY ( ensure ( j, S_SEQSTART, T, &seq_start ) );
+    MTX_TRY ( ensure ( j, S_XOFF, ( size_t ) NS * NG, &xoff ) );
+    for ( uint32_t b = 0; b <= NG; ++b )
+        MTX_LAUNCH ( k_wplanes_all, blocks_for ( T, 256 ), 256, codes, T, b ? j->blens[b - 1] : P.l, ( uint32_t ) B,
+                     ed ? 0 : 1, wpl + ( size_t ) b * B * T );
+    MTX_LAUNCH ( k_struct_rows, blocks_for ( T, 256 ), 256, dptr<uint32_t> ( j, S_OFFS ), j->nseq, j->total, P.l,
+                 j->tml, ( int ) j->pair_mode, row_ok, row_end );
+    MTX_LAUNCH ( k_seq_start, blocks_for ( T, 256 ), 256, dptr<uint32_t> ( j, S_OFFS ), j->nseq, j->total, seq_start );
+    // cumulative end offsets of boxes 1..NG for every structure k (motex.cc:439-486 order)
+    uint32_t * h_xoff = pin<uint32_t> ( j, kPinXoff );
+    for ( uint32_t k = 0; k < NS; ++k )
+    {
+        uint32_t rem = k, off = 0;
+        std::vector<uint32_t> S ( NG );
+        for ( int g = ( int ) NG - 1; g >= 0; --g )
+        {
+            const uint32_t span = j->gmax[g] - j->gmin[g] + 1;
+            S[g] = j->gmin[g] + rem % span;
+            rem /= span;
+        }
+        for ( uint32_t g = 0; g < NG; ++g )
+        {
+            off += S[g] + j->blens[g];
+            h_xoff[k * NG + g] = off;
+        }
+    }
+    MTX_CUDA ( cudaMemcpyAsync ( xoff, h_xoff, ( size_t ) NS * NG * 4, cudaMemcpyHostToDevice, st ) );
+    const uint32_t ctas_x = ( T + kDPThreads - 1 ) / kDPThreads;
+    j->ntiles = ctas_x;
+    const uint32_t first_blk = j->pair_mode ? ( j->offs[1] / 32 ) : 0;
+    const uint32_t warmup = ed ? P.l + P.e - 1 : 0;
+    uint32_t nchunks = std::max<uint32_t> ( 1, ( ( uint32_t ) j->ctx->num_sms * 24 + ctas_x - 1 ) / ctas_x );
+    nchunks = std::min<uint32_t> ( nchunks, std::max<uint32_t> ( 1, ( j->nblk - first_blk ) / 16 ) );
+    build_chunks ( j, first_blk, nchunks, warmup, j->chunks );
+    ChunkInfo * d_chunks;
+    MTX_TRY ( upload_chunks ( j, &d_chunks ) );
+    uint64_t scanned = 0;
+    for ( auto & ch : j->chunks ) scanned += ( uint64_t ) ( ch.end - ch.warm ) * 32;
+    j->exec_cells = ( uint64_t ) T * scanned * ( NG + 1 );
+    const uint64_t n = ( uint64_t ) T * NS;
+    if ( n >= 0xffffff00ull ) return fail ( MOTEX_EUNSUPPORTED, "positions x gap structures exceeds 2^32" );
+    uint32_t *u_acc, *v_acc;
+    uint8_t * flags;
+    MTX_TRY ( ensure ( j, S_UACC, n, &u_acc ) );
+    MTX_TRY ( ensure ( j, S_VACC, n, &v_acc ) );
+    MTX_TRY ( ensure ( j, S_FLAGS, std::max<uint64_t> ( 1, j->n_split ) * n, &flags ) );
+    MTX_CUDA ( cudaMemsetAsync ( u_acc, 0, n * 4, st ) );
+    MTX_CUDA ( cudaMemsetAsync ( v_acc, 0, n * 4, st ) );
+    if ( j->n_split ) MTX_CUDA ( cudaMemsetAsync ( flags, 0, ( size_t ) j->n_split * n, st ) );
+    StructNArgs & sa = j->san;
+    sa = StructNArgs {};
+    sa.text.planes = dptr<uint32_t> ( j, S_PLANES );
+    sa.text.plane_stride = j->stride;
+    sa.text.vmask = dptr<uint32_t> ( j, S_VMASK );
+    sa.text.emask = dptr<uint32_t> ( j, S_EMASK );
+    sa.text.nblk = j->nblk;
+    sa.wpl = wpl;
+    sa.row_ok = row_ok;
+    sa.row_end = row_end;
+    sa.seq_start = seq_start;
+    sa.xoff = xoff;
+    sa.total = T;
+    sa.l0 = P.l;
+    sa.e0 = P.e;
+    sa.blen[0] = P.l;
+    sa.berr[0] = P.e;
+    for ( uint32_t g = 0; g < NG; ++g )
+    {
+        sa.blen[g + 1] = j->blens[g];
+        sa.berr[g + 1] = j->berrs[g];
+    }
+    sa.ngaps = NG;
+    sa.nstructs = NS;
+    sa.chunks = d_chunks;
+    sa.u_acc = u_acc;
+    sa.v_acc = v_acc;
+    sa.split_flags = flags;
+    j->U = T;
+    j->dp_pending = true;
+    return MOTEX_OK;
+}
+
 // DP of one job as its own (static-grid) launch.
 int stage_dp ( Job * j )
 {
@@ -693,7 +966,9 @@ int stage_dp ( Job * j )
     const bool ed = j->prm.d == 1;
     MTX_TRY ( record ( j, j->evd0 ) );
     bool ok;
-    if ( j->structured )
+    if ( j->structured && j->structN )
+        ok = launch_dp_structN ( j->san, j->B, ed, dim3 ( j->ntiles, ( unsigned ) j->chunks.size () ), st );
+    else if ( j->structured )
         ok = launch_dp_struct1 ( j->sa, j->B, ed, dim3 ( j->ntiles, ( unsigned ) j->chunks.size () ), st );
     else
     {
@@ -914,7 +1189,8 @@ int load_job ( Job * j, const motex_params * prm, const char * const * seqs, con
     j->prm.gap_max = j->gmax.data ();
     j->prm.blens = j->blens.data ();
     j->prm.berrs = j->berrs.data ();
-    j->G = prm->nb_gaps ? j->gmax[0] - j->gmin[0] + 1 : 1;
+    j->G = 1;                                      // gap structures (lexicographic, gap 0 slowest)
+    for ( uint32_t g = 0; g < prm->nb_gaps; ++g ) j->G *= j->gmax[g] - j->gmin[g] + 1;
     j->nseq = nseq;
     j->pair_mode = pair_mode;
     j->offs.assign ( nseq + 1, 0 );
@@ -1016,12 +1292,25 @@ int fetch_records ( Job * j, motex_result * out )
         while ( j->offs[s + 1] <= pos ) ++s;        // records are in (position, gap choice) order
         if ( j->prm.nb_gaps )
         {
-            // the writer's key: box 0 and box 1 joined by '_', gap left out
+            // the writer's key: the boxes joined by '_', gaps left out
             // (functions.cc:1191-1239); the first passing entry of a key wins
-            const uint32_t l = j->prm.l, b1 = j->blens[0], gap = j->gmin[0] + k;
-            key.assign ( j->raw_host.data () + pos + 1 - l, l );
-            key.push_back ( '_' );
-            key.append ( j->raw_host.data () + pos + 1 + gap, b1 );
+            const uint32_t l = j->prm.l, NG = j->prm.nb_gaps;
+            const char * x = j->raw_host.data ();
+            key.assign ( x + pos + 1 - l, l );
+            uint32_t rem = k, end = pos;
+            uint32_t S[kMaxGapsN];
+            for ( int g = ( int ) NG - 1; g >= 0; --g )
+            {
+                const uint32_t span = j->gmax[g] - j->gmin[g] + 1;
+                S[g] = j->gmin[g] + rem % span;
+                rem /= span;
+            }
+            for ( uint32_t g = 0; g < NG; ++g )
+            {
+                key.push_back ( '_' );
+                key.append ( x + end + 1 + S[g], j->blens[g] );
+                end += S[g] + j->blens[g];
+            }
             if ( ! seen.insert ( key ).second ) continue;
         }
         out->motifs[kept++] = motex_motif { s, pos - j->offs[s], k, h[3 * i + 1], h[3 * i + 2] };
@@ -1249,6 +1538,7 @@ int motex_gpu_run_batch ( motex_ctx * c, const motex_job * jobs, uint32_t njobs,
     {
         js[i] = c->pool[i].get ();
         js[i]->replaying = false;
+        js[i]->batched = true;
         MTX_TRY ( load_job ( js[i], jobs[i].prm, jobs[i].seqs, jobs[i].lens, jobs[i].nseq, false ) );
     }
     for ( Job * j : js ) MTX_TRY ( stage_presence ( j ) );

@@ -242,6 +242,43 @@ extern "C" int oracle_extract_pair ( int d, unsigned l, unsigned e, const char *
     return 1;
 }
 
+/* structured_motifs_extraction_hd/_ed for one pair (functions.cc:564-705,
+ * 773-915): u, v hold m * nb_structs entries, [k * m + j], accumulated. */
+extern "C" int oracle_extract_pair_struct ( int d, unsigned l, unsigned e, unsigned nb_gaps, const unsigned * gmin,
+                                            const unsigned * gmax, const unsigned * blens, const unsigned * berrs,
+                                            const char * p, unsigned m, const char * t, unsigned n,
+                                            unsigned * u, unsigned * v )
+{
+    std::vector<std::string> s { std::string ( p, m ), std::string ( t, n ) };
+    Coded C = encode ( s );
+    Params P;
+    P.l = l; P.e = e; P.d = ( unsigned ) d;
+    P.nb_gaps = nb_gaps;
+    P.nb_boxes = nb_gaps + 1;
+    P.blens.assign ( blens, blens + nb_gaps );
+    P.berrs.assign ( berrs, berrs + nb_gaps );
+    P.nb_structs = 1;
+    for ( unsigned g = 0; g < nb_gaps; ++g ) P.nb_structs *= gmax[g] - gmin[g] + 1;
+    P.S.assign ( P.nb_structs, std::vector<unsigned> ( nb_gaps ) );
+    for ( unsigned k = 0; k < P.nb_structs; ++k )
+    {
+        unsigned rem = k;
+        for ( int g = ( int ) nb_gaps - 1; g >= 0; --g )
+        {
+            unsigned span = gmax[g] - gmin[g] + 1;
+            P.S[k][g] = gmin[g] + rem % span;
+            rem /= span;
+        }
+    }
+    std::vector<std::vector<uint64_t>> peqs ( P.nb_boxes );
+    if ( d == 1 )
+        for ( unsigned b = 0; b < P.nb_boxes; ++b ) build_peq ( C.seq[0], b ? P.blens[b - 1] : l, C.sigma, peqs[b] );
+    std::vector<std::vector<unsigned>> B;
+    std::vector<unsigned char> occ;
+    extract_structured ( P, C.seq[0], C.seq[1], d == 1 ? &peqs : nullptr, C.sigma, u, v, B, occ );
+    return 1;
+}
+
 /* u, v of one word over all searched sequences (length >= tml) of a set:
  * the per-word totals the all-pairs driver accumulates (motex.cc:531-581). */
 extern "C" int oracle_word_uv ( int d, unsigned l, unsigned e, const char * word, const char * text,

@@ -70,6 +70,40 @@ def planted_structured(seed, nseq, length, d):
                       boxes=((5, 15, 10, 1),))
 
 
+def planted_structured2(seed, nseq, length, d):
+    """A planted 3-box structured motif (6-mer, gap 3-5, 7-mer, gap 2-3,
+    6-mer; <= 1 substitution per box) in 60% of the sequences: two gaps."""
+    rng = np.random.default_rng(seed)
+    seqs = [W._rand_seq(rng, W.DNA, length) for _ in range(nseq)]
+    b0, b1, b2 = (W._rand_seq(rng, W.DNA, n) for n in (6, 7, 6))
+
+    def copy():
+        g1 = W._rand_seq(rng, W.DNA, int(rng.integers(3, 6)))
+        g2 = W._rand_seq(rng, W.DNA, int(rng.integers(2, 4)))
+        return (W._substitute(rng, b0, W.DNA, int(rng.integers(2))) + g1 +
+                W._substitute(rng, b1, W.DNA, int(rng.integers(2))) + g2 +
+                W._substitute(rng, b2, W.DNA, int(rng.integers(2))))
+    W._plant(rng, seqs, copy, 0.6)
+    return W.Workload("planted_structured2", "DNA", seqs, d=d, k=6, e=1, q=25,
+                      boxes=((3, 5, 7, 1), (2, 3, 6, 1)))
+
+
+def planted_long_gap(seed, nseq, length, d):
+    """One gap of 20-30 symbols between a 7-mer and an 8-mer: a gap longer
+    than the box-0 hit history of the one-gap kernel."""
+    rng = np.random.default_rng(seed)
+    seqs = [W._rand_seq(rng, W.DNA, length) for _ in range(nseq)]
+    b0, b1 = W._rand_seq(rng, W.DNA, 7), W._rand_seq(rng, W.DNA, 8)
+
+    def copy():
+        gap = W._rand_seq(rng, W.DNA, int(rng.integers(20, 31)))
+        return (W._substitute(rng, b0, W.DNA, int(rng.integers(2))) + gap +
+                W._substitute(rng, b1, W.DNA, int(rng.integers(2))))
+    W._plant(rng, seqs, copy, 0.5)
+    return W.Workload("planted_long_gap", "DNA", seqs, d=d, k=7, e=1, q=30,
+                      boxes=((20, 30, 8, 1),))
+
+
 def quorum_boundary(seed):
     """100 sequences; one 10-mer planted exactly in 29 of them and run with
     q=29: (29/100)*100 evaluates below 29 in IEEE double, so the reference
@@ -142,6 +176,10 @@ def cases():
     out.append(("struct_ed_dna_ed_12seq", W.structured(seed=2, scale=0.01, d=1), [], None))
     out.append(("struct_planted_hd", planted_structured(11, 16, 150, 0), [], None))
     out.append(("struct_planted_ed", planted_structured(11, 16, 150, 1), [], None))
+    out.append(("struct2_planted_hd", planted_structured2(22, 14, 160, 0), [], None))
+    out.append(("struct2_planted_ed", planted_structured2(22, 14, 160, 1), [], None))
+    out.append(("struct_long_gap_hd", planted_long_gap(23, 12, 150, 0), [], None))
+    out.append(("struct_long_gap_ed", planted_long_gap(23, 12, 150, 1), [], None))
     out.append(("quorum_boundary_q29", quorum_boundary(12), [], None))
     out.append(("dna_with_N_hd", with_n(13, 0), [], None))
     out.append(("dna_with_N_ed", with_n(13, 1), [], None))

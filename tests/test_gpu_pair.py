@@ -55,3 +55,43 @@ def test_pair_accumulates(native_built, gpu_ctx, oracle_port):
     u1, v1 = oracle_pair(1, 6, 1, p, t1)
     u2, v2 = oracle_pair(1, 6, 1, p, t2)
     assert u == [a + b for a, b in zip(u1, u2)] and v == [a + b for a, b in zip(v1, v2)]
+
+
+def oracle_pair_struct(d, l, e, boxes, p, t):
+    lib = C.CDLL(PORT_LIB)
+    ng = len(boxes)
+    cols = [(C.c_uint * ng)(*[b[i] for b in boxes]) for i in range(4)]
+    ns = 1
+    for g in boxes:
+        ns *= g[1] - g[0] + 1
+    U = (C.c_uint32 * (len(p) * ns))()
+    V = (C.c_uint32 * (len(p) * ns))()
+    lib.oracle_extract_pair_struct(d, l, e, ng, cols[0], cols[1], cols[2], cols[3], p.encode(), len(p),
+                                   t.encode(), len(t), U, V)
+    return list(U), list(V), ns
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("d", [0, 1])
+def test_pair_structured(native_built, gpu_ctx, oracle_port, d):
+    """structured_motifs_extraction_hd/_ed drop-in: one gap (shared-history
+    kernel), a long gap and two gaps (box-check kernel)."""
+    rng = random.Random(300 + d)
+    shapes = [((6, 4, 1), ((2, 6, 5, 1),)), ((7, 1, 0), ((20, 26, 6, 1),)),
+              ((5, 1, 1), ((1, 3, 5, 1), (2, 3, 4, 0))), ((8, 2, 2), ((4, 9, 7, 2),))]
+    for case in range(24):
+        (l, _, e), boxes = shapes[case % len(shapes)]
+        e = min(e, l - 1)
+        m, n = rng.randint(60, 160), rng.randint(60, 200)
+        p = "".join(rng.choice("ACGT") for _ in range(m))
+        t = "".join(rng.choice("ACGT") for _ in range(n))
+        # plant one copy of a structured occurrence of p into t
+        a = rng.randint(0, m - 45)
+        seg = p[a:a + 45]
+        b = rng.randint(0, n - 45)
+        t = t[:b] + seg + t[b + 45:]
+        U, V, ns = oracle_pair_struct(d, l, e, boxes, p, t)
+        prm = native_built.make_params(d, l, e, boxes=boxes)
+        got = gpu_ctx.extract_pair(p, t, prm, nb_structs=ns)
+        assert got == (U, V), (case, d, l, e, boxes)
+        assert sum(V) > 0

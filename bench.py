@@ -51,6 +51,8 @@ WORKLOADS = {
     "prot_uneven_d0": lambda s: W.prot_uneven(d=0, scale=s),
     "prot_uneven_d1": lambda s: W.prot_uneven(d=1, scale=s),
     "dna_long": lambda s: W.dna_long(scale=s),
+    "structured_d1": lambda s: W.structured(scale=s, d=1),
+    "structured_d0": lambda s: W.structured(scale=s, d=0),
 }
 DEFAULT_WORKLOAD = "dna_ed"
 # algorithmic integer operations per DP cell (one factor x one text position)
@@ -190,7 +192,8 @@ def traffic_record(workload):
     try:
         with open(os.path.join(ROOT, "profiles", "dp_traffic.json")) as f:
             rec = json.load(f)
-        return rec.get(workload)
+        r = rec.get(workload)
+        return None if r is None else r.get("traffic")
     except (OSError, ValueError):
         return None
 

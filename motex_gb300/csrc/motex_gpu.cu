@@ -394,10 +394,11 @@ DPTune choose_tune ( Job * j, uint32_t U, bool ed, bool generic )
  * (bit planes B, factor length l, errors e, distance d) has no entry yet,
  * every candidate launch shape -- register words per thread W, factors per
  * register NL (SWAR or 1-lane for edit distance), block unroll UR -- runs the
- * DP on a probe: one full wave of tiles (at most 8 per SM) over a 512-block
- * text chunk, long enough that the per-CTA set-up weighs as little as in the
- * real run; time per cell from CUDA events picks the winner, accumulators
- * are cleared afterwards.  Batched jobs are not tuned (the persistent kernels
+ * DP on a probe grid: up to 8 tiles per SM times as many 512-block text
+ * chunks as fill every SM's CTA slots several times, like the real grid, and
+ * long enough that the per-CTA set-up weighs as little as in the real run;
+ * time per cell from CUDA events picks the winner; accumulators are cleared
+ * afterwards.  Batched jobs are not tuned (the persistent kernels
  * have a fixed shape).  Entries are shared by every context of the
  * process and, with MOTEX_TUNE_CACHE=<file>, read from and appended to that
  * file.  MOTEX_AUTOTUNE=0 turns tuning off (the defaults of choose_tune
@@ -473,13 +474,14 @@ int autotune ( Job * j, DPTune * best )
                 cands.push_back ( DPTune { W, NL, UR } );
         if ( NL == 1 ) break;
     }
-    // probe chunk: 64 blocks from the start of the text, no splits
-    ChunkInfo probe { 0, 0, std::min<uint32_t> ( j->nblk, kTuneBlocks ), -1, -1 };
+    // probe chunks: consecutive 512-block ranges from the start of the text, no splits
+    const uint32_t pblk = std::min<uint32_t> ( j->nblk, kTuneBlocks );
+    const uint32_t maxc = std::max<uint32_t> ( 1, std::min<uint32_t> ( 16, j->nblk / pblk ) );
     ChunkInfo * d_probe;
-    MTX_TRY ( ensure ( j, S_TILES, ( sizeof ( ChunkInfo ) + 3 ) / 4, reinterpret_cast<uint32_t **> ( &d_probe ) ) );
+    MTX_TRY ( ensure ( j, S_TILES, maxc * ( ( sizeof ( ChunkInfo ) + 3 ) / 4 ), reinterpret_cast<uint32_t **> ( &d_probe ) ) );
     ChunkInfo * h_probe = pin<ChunkInfo> ( j, kPinChunks );
-    *h_probe = probe;
-    MTX_CUDA ( cudaMemcpyAsync ( d_probe, h_probe, sizeof probe, cudaMemcpyHostToDevice, j->ctx->st ) );
+    for ( uint32_t c = 0; c < maxc; ++c ) h_probe[c] = ChunkInfo { c * pblk, c * pblk, ( c + 1 ) * pblk, -1, -1 };
+    MTX_CUDA ( cudaMemcpyAsync ( d_probe, h_probe, maxc * sizeof ( ChunkInfo ), cudaMemcpyHostToDevice, j->ctx->st ) );
     DPArgs da = j->da;
     da.chunks = d_probe;
     float best_ms = 1e30f;
@@ -487,7 +489,10 @@ int autotune ( Job * j, DPTune * best )
     {
         const uint32_t groups = ( j->U + t.NL - 1 ) / t.NL;
         const uint32_t ntiles = ( groups + kDPThreads * t.W - 1 ) / ( kDPThreads * t.W );
-        const dim3 grid ( std::min<uint32_t> ( ntiles, 8u * j->ctx->num_sms ), 1 );
+        // enough CTAs to fill every SM's slots several times, like the real grid
+        const uint32_t gx = std::min<uint32_t> ( ntiles, 8u * j->ctx->num_sms );
+        const uint32_t gy = std::min<uint32_t> ( maxc, std::max<uint32_t> ( 1, ( 16u * j->ctx->num_sms + gx - 1 ) / gx ) );
+        const dim3 grid ( gx, gy );
         for ( int rep = 0; rep < 2; ++rep )                     // first launch warms up
         {
             MTX_TRY ( record ( j, j->evd0 ) );
@@ -498,8 +503,9 @@ int autotune ( Job * j, DPTune * best )
         MTX_CUDA ( cudaEventSynchronize ( j->evd1 ) );
         float ms = 0.f;
         MTX_CUDA ( cudaEventElapsedTime ( &ms, j->evd0, j->evd1 ) );
-        // normalise by the factors the probe covered
-        const double per = ms / ( double ) std::min<uint64_t> ( ( uint64_t ) grid.x * kDPThreads * t.W * t.NL, j->U );
+        // time per cell the probe covered
+        const double per = ms / ( ( double ) std::min<uint64_t> ( ( uint64_t ) grid.x * kDPThreads * t.W * t.NL, j->U ) *
+                                  grid.y * pblk * 32.0 );
         if ( per < best_ms ) { best_ms = ( float ) per; *best = t; }
     }
     std::lock_guard<std::mutex> lk ( g_tune_mu );

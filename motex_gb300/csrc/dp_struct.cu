@@ -17,6 +17,9 @@
 // [gmin+b1, gmax+b1]) to v[k, P0+lane] -- all text gap choices at once.
 #include "kernels.cuh"
 
+#include <algorithm>
+#include <cstdlib>
+
 namespace mtx
 {
 
@@ -201,11 +204,192 @@ __global__ void __launch_bounds__ ( kDPThreads ) k_dp_struct1 ( const StructArgs
     }
 }
 
+/*
+ * Edit distance with the lane's three rows -- box 0 (length l0) and its two
+ * box-1 rows (length b1) -- packed in one 32-bit register: SWAR lanes of
+ * different lengths at offsets 0, oB = l0+1, oC = oB+b1+1, a guard bit above
+ * each.  The guard invariants of the single-motif SWAR kernel keep the lanes
+ * apart; the score of each lane sits in a bit field shifted down by the
+ * common s = min(l0, b1) - 1 from the lane's top bit, and the hit test reads
+ * each lane's top bit after adding 2^s - (e+1) per field, which needs
+ * e + 1 <= 2^s and l - e - 1 < 2^s per lane.
+ */
+struct HSwarConst
+{
+    uint32_t HB, NG, NGm1, K, SC0, s;
+    uint32_t bitA, bitB, bitC;      // top bit of box 0, row r0, row r1
+    uint32_t oB, oC;
+};
+
+bool hswar_shape ( const StructArgs & a, HSwarConst * C )
+{
+    const uint32_t Ls[3] = { a.l0, a.b1, a.b1 }, es[3] = { a.e0, a.e1, a.e1 };
+    const uint32_t oB = a.l0 + 1, oC = oB + a.b1 + 1;
+    if ( oC + a.b1 > 32 ) return false;
+    const uint32_t s = std::min ( a.l0, a.b1 ) - 1;
+    if ( s < 1 || s > 30 ) return false;
+    const uint32_t offs[3] = { 0, oB, oC };
+    C->HB = C->K = C->SC0 = 0;
+    uint32_t guards = 0;
+    for ( int i = 0; i < 3; ++i )
+    {
+        if ( es[i] + 1 > ( 1u << s ) || Ls[i] - es[i] - 1 >= ( 1u << s ) ) return false;
+        const uint32_t hb = offs[i] + Ls[i] - 1, f = hb - s;
+        C->HB |= 1u << hb;
+        if ( offs[i] + Ls[i] < 32 ) guards |= 1u << ( offs[i] + Ls[i] );
+        C->K += ( ( 1u << s ) - ( es[i] + 1 ) ) << f;
+        C->SC0 += Ls[i] << f;
+    }
+    C->NG = ~guards;
+    C->NGm1 = C->NG & ~C->HB;
+    C->s = s;
+    C->bitA = 1u << ( a.l0 - 1 );
+    C->bitB = 1u << ( oB + a.b1 - 1 );
+    C->bitC = 1u << ( oC + a.b1 - 1 );
+    C->oB = oB;
+    C->oC = oC;
+    return true;
+}
+
+template <int B>
+__global__ void __launch_bounds__ ( kDPThreads ) k_dp_struct1_swar ( const StructArgs a, const HSwarConst C )
+{
+    extern __shared__ uint32_t smem[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t G = a.G;
+    uint32_t * s_cnt = smem + ( size_t ) threadIdx.x * G * 3;
+    uint32_t * s_u = s_cnt + G;
+    uint32_t * s_v = s_u + G;
+    for ( uint32_t k = 0; k < G; ++k ) s_cnt[k] = s_u[k] = s_v[k] = 0;
+
+    const uint32_t P0 = ( blockIdx.x * ( kDPThreads / 32 ) + warp ) * 32;
+    const uint32_t jx = P0 + lane;
+    const uint32_t r0 = P0 + a.gmin + a.b1 + lane;
+    const uint32_t r1 = r0 + 32;
+    const bool has_r1 = lane + 1 < ( int ) G;
+    uint32_t w[B];
+#pragma unroll
+    for ( int b = 0; b < B; ++b )
+    {
+        const uint32_t x0 = jx < a.total ? a.wpl0[( size_t ) b * a.total + jx] : 0u;
+        const uint32_t x1 = r0 < a.total ? a.wpl1[( size_t ) b * a.total + r0] : 0u;
+        const uint32_t x2 = ( has_r1 && r1 < a.total ) ? a.wpl1[( size_t ) b * a.total + r1] : 0u;
+        w[b] = x0 | ( x1 << C.oB ) | ( x2 << C.oC );
+    }
+    uint32_t kvalid = 0;
+    if ( jx < a.total && a.row_ok[jx] )
+    {
+        const uint32_t xend = a.row_end[jx];
+        for ( uint32_t k = 0; k < G; ++k )
+            if ( jx + a.gmin + k + a.b1 < xend ) kvalid |= 1u << k;
+    }
+    const uint32_t Gmask = G >= 32 ? 0xffffffffu : ( ( 1u << G ) - 1u );
+    const uint32_t win = ( ( a.gmax + a.b1 >= 31 ) ? 0xffffffffu : ( ( 2u << ( a.gmax + a.b1 ) ) - 1u ) ) &
+                         ~( ( 1u << ( a.gmin + a.b1 ) ) - 1u );
+    const uint32_t bitC = has_r1 ? C.bitC : 0u;
+    const ChunkInfo ch = a.chunks[blockIdx.y];
+    int cur_split = ch.first_split;
+    const uint32_t * __restrict__ planes = a.text.planes;
+    const uint32_t stride = a.text.plane_stride;
+    const uint32_t sh = C.s;
+    uint32_t hist = 0, Pv = C.NG, Mv = 0, sc = C.SC0;
+
+    auto flush = [&] () {
+        for ( uint32_t k = 0; k < G; ++k )
+        {
+            const uint32_t c = s_cnt[k];
+            if ( ! c ) continue;
+            if ( cur_split < 0 ) s_u[k] += 1;
+            else if ( jx < a.total ) a.split_flags[( ( size_t ) cur_split * a.total + jx ) * G + k] = 1;
+            s_v[k] += c;
+            s_cnt[k] = 0;
+        }
+    };
+
+    for ( uint32_t kb = ch.warm; kb < ch.end; ++kb )
+    {
+        uint32_t cur[B];
+#pragma unroll
+        for ( int b = 0; b < B; ++b ) cur[b] = __ldg ( planes + ( size_t ) b * stride + kb + 1 );
+        const uint32_t vm = __ldg ( a.text.vmask + kb ), em = __ldg ( a.text.emask + kb );
+        const bool counting = kb >= ch.begin;
+#pragma unroll 4
+        for ( int r = 0; r < 32; ++r )
+        {
+            uint32_t x = 0;
+#pragma unroll
+            for ( int b = 0; b < B; ++b ) x |= w[b] ^ ( ( 0u - ( ( cur[b] >> r ) & 1u ) ) & C.NG );
+            const uint32_t Xv = ~x | Mv;
+            const uint32_t s1 = ( ~x & Pv ) + Pv;
+            const uint32_t Xh = ( s1 ^ Pv ) | ~x;
+            const uint32_t Ph = Mv | ~( Xh | Pv );
+            const uint32_t Mhs = Pv & Xh & C.NGm1;
+            const uint32_t mh = Pv & Xh & C.HB;
+            const uint32_t ph = Ph & C.HB;
+            sc = sc + ( ph >> sh ) - ( mh >> sh );
+            const uint32_t Ph2 = Ph << 1, Mh2 = Mhs << 1;
+            Pv = Mh2 | ~( Xv | Ph2 );
+            Mv = Ph2 & Xv & C.NG;
+            const uint32_t hits = ~( sc + C.K ) & C.HB;
+            const bool h0 = ( hits & C.bitA ) && ( ( vm >> r ) & 1u );
+            hist = ( hist << 1 ) | ( uint32_t ) h0;
+            const uint32_t Ha = __ballot_sync ( 0xffffffffu, hits & C.bitB );
+            const uint32_t Hb = __ballot_sync ( 0xffffffffu, hits & bitC );
+            if ( counting && ( Ha | Hb ) )
+            {
+                const uint64_t H = ( ( uint64_t ) Hb << 32 ) | Ha;
+                const uint32_t g = ( uint32_t ) ( H >> lane ) & Gmask & kvalid;
+                if ( g )
+                {
+                    const uint32_t c = __popc ( hist & win );
+                    if ( c )
+                        for ( uint32_t k = 0; k < G; ++k )
+                            if ( ( g >> k ) & 1u ) s_cnt[k] += c;
+                }
+            }
+            if ( ( em >> r ) & 1u )
+            {
+                if ( counting )
+                {
+                    flush ();
+                    cur_split = -1;
+                }
+                hist = 0;
+                Pv = C.NG;
+                Mv = 0;
+                sc = C.SC0;
+            }
+        }
+    }
+    for ( uint32_t k = 0; k < G; ++k )
+    {
+        const uint32_t c = s_cnt[k];
+        if ( c )
+        {
+            if ( ch.last_split >= 0 && jx < a.total )
+                a.split_flags[( ( size_t ) ch.last_split * a.total + jx ) * G + k] = 1;
+            else
+                s_u[k] += 1;
+            s_v[k] += c;
+        }
+        if ( jx < a.total && ( s_u[k] | s_v[k] ) )
+        {
+            atomicAdd ( a.u_acc + ( size_t ) jx * G + k, s_u[k] );
+            atomicAdd ( a.v_acc + ( size_t ) jx * G + k, s_v[k] );
+        }
+    }
+}
+
 template <int B>
 static void launch_struct_b ( const StructArgs & a, bool ed, dim3 grid, size_t smem, cudaStream_t st )
 {
-    if ( ed ) k_dp_struct1<B, true><<<grid, kDPThreads, smem, st>>> ( a );
-    else k_dp_struct1<B, false><<<grid, kDPThreads, smem, st>>> ( a );
+    HSwarConst C;
+    if ( ed && ! getenv ( "MOTEX_STRUCT_NO_SWAR" ) && hswar_shape ( a, &C ) )
+        k_dp_struct1_swar<B><<<grid, kDPThreads, smem, st>>> ( a, C );
+    else if ( ed )
+        k_dp_struct1<B, true><<<grid, kDPThreads, smem, st>>> ( a );
+    else
+        k_dp_struct1<B, false><<<grid, kDPThreads, smem, st>>> ( a );
 }
 
 bool launch_dp_struct1 ( const StructArgs & a, int B, bool ed, dim3 grid, cudaStream_t st )
@@ -216,7 +400,7 @@ bool launch_dp_struct1 ( const StructArgs & a, int B, bool ed, dim3 grid, cudaSt
     if ( smem > 48 * 1024 ) return false;
     switch ( B )
     {
-        case 1: launch_struct_b<1> ( a, ed, grid, smem, st ); return true;
+        case 1:
         case 2: launch_struct_b<2> ( a, ed, grid, smem, st ); return true;
         case 3: launch_struct_b<3> ( a, ed, grid, smem, st ); return true;
         case 4: launch_struct_b<4> ( a, ed, grid, smem, st ); return true;

@@ -77,9 +77,12 @@ def test_pair_structured(native_built, gpu_ctx, oracle_port, d):
     """structured_motifs_extraction_hd/_ed drop-in: one gap (shared-history
     kernel), a long gap and two gaps (box-check kernel)."""
     rng = random.Random(300 + d)
+    # one gap packed in one register (edit distance), one gap that does not fit the
+    # packed lanes, a long gap and two gaps (box-check kernel)
     shapes = [((6, 4, 1), ((2, 6, 5, 1),)), ((7, 1, 0), ((20, 26, 6, 1),)),
-              ((5, 1, 1), ((1, 3, 5, 1), (2, 3, 4, 0))), ((8, 2, 2), ((4, 9, 7, 2),))]
-    for case in range(24):
+              ((5, 1, 1), ((1, 3, 5, 1), (2, 3, 4, 0))), ((8, 2, 2), ((4, 9, 7, 2),)),
+              ((12, 3, 2), ((2, 5, 12, 2),))]
+    for case in range(30):
         (l, _, e), boxes = shapes[case % len(shapes)]
         e = min(e, l - 1)
         m, n = rng.randint(60, 160), rng.randint(60, 200)

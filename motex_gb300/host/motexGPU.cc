@@ -13,10 +13,14 @@
  *   boxes file              motex.cc:302-363
  *   header                  functions.cc:1010-1068
  *   motif lines and footer  functions.cc:1118-1129, 1238-1247
+ *   SMILE-like file (-S)    functions.cc:1262-1461 (header, plain motifs)
+ *                           and 1463-1591 (structured motifs)
+ *   option combinations     motex.cc:147-201
  * Differences: -L <int> is accepted as a real switch (the reference compiles
  * it out and getopt reports it as invalid; the output is the same), -t is
- * accepted and ignored, and the statistics / SMILE modes (-b -u -U -I -S)
- * are not part of this tool.
+ * accepted and ignored, and the background / unmatched-motif modes
+ * (-b -u -U -I) are rejected after the reference's own checks of their
+ * combinations.
  *
  * Set MOTEX_METRICS=<file> to append a JSON line with the run's cell counts,
  * device time and GCUPS.
@@ -25,6 +29,7 @@
 
 #include <ctype.h>
 #include <getopt.h>
+#include <math.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
@@ -101,6 +106,8 @@ static void usage ( void )
                       "                                      (default: 10000).\n" );
     fprintf ( stdout, "  -s, --structured-motifs   <str>     Input filename  for the structure of the\n"
                       "                                      boxes in the case of structured motifs.\n" );
+    fprintf ( stdout, "  -S, --SMILE-out-file      <str>     SMILE-like output filename to be used by\n"
+                      "                                      SMILE.\n" );
     fprintf ( stdout, "  -L, --long-sequences      <int>     Accepted for compatibility; the GPU tiles\n"
                       "                                      long sequences by itself.\n" );
     fprintf ( stdout, "  -t, --threads             <int>     Accepted for compatibility (ignored).\n" );
@@ -184,6 +191,76 @@ static void write_header ( FILE * out, const Switches & sw, const motex_params &
     fprintf ( out, "####################################\n\n" );
 }
 
+/*
+ * SMILE-like output (functions.cc:1262-1345 header, 1368-1461 plain motifs,
+ * 1463-1591 structured motifs).  The header line starts with "%%%", gives the
+ * box count, the absolute quorum ceil(q * num_seqs / 100) over num_seqs, the
+ * total input length and, per box, length range and error budget, then the
+ * alphabet; DNA pads it to 79 columns and adds two blank 79-column lines,
+ * PROT pads to 159 columns and adds one, USR adds nothing before the rule of
+ * '='.  Each motif line is the word (boxes joined by '_'), its symbol-index
+ * string ('0' + rank in the alphabet string, '-' for a separator), u, a tab
+ * and v.  The motif set and order are those of the main output.
+ */
+static void write_smile ( FILE * out, const Switches & sw, const motex_params & P, unsigned num_seqs,
+                          unsigned total_length, const char * alphabet, const std::vector<std::string> & words,
+                          const motex_result & res, double secs )
+{
+    char buf[128];
+    const int quorum = ( int ) ceil ( ( double ) ( ( double ) sw.q * num_seqs ) / ( double ) 100 );
+    std::string line;
+    if ( P.nb_gaps == 0 )
+    {
+        snprintf ( buf, sizeof buf, "%%%%%% 1 %d/%d %d %d %d %d alphabet ", quorum, num_seqs, total_length, sw.l, sw.l, sw.e );
+        line = buf;
+    }
+    else
+    {
+        unsigned len = sw.l, errs = sw.e;
+        for ( unsigned g = 0; g < P.nb_gaps; ++g ) { len += P.blens[g]; errs += P.berrs[g]; }
+        snprintf ( buf, sizeof buf, "%%%%%% %d %d/%d %d %d %d %d %d %d %d ", P.nb_gaps + 1, quorum, num_seqs, total_length,
+                   len, len, errs, sw.l, sw.l, sw.e );
+        line = buf;
+        for ( unsigned g = 0; g < P.nb_gaps; ++g )
+        {
+            snprintf ( buf, sizeof buf, "%d %d %d %d %d ", P.gap_min[g], P.gap_max[g], P.blens[g], P.blens[g], P.berrs[g] );
+            line += buf;
+        }
+        line += "alphabet ";
+    }
+    line += alphabet;
+    line += '$';
+    fputs ( line.c_str (), out );
+    const std::string blank ( 79, ' ' );
+    if ( ! strcmp ( sw.alphabet, "DNA" ) )
+    {
+        if ( line.size () < 79 ) fputs ( std::string ( 79 - line.size (), ' ' ).c_str (), out );
+        fprintf ( out, "\n%s\n%s\n", blank.c_str (), blank.c_str () );
+    }
+    if ( ! strcmp ( sw.alphabet, "PROT" ) )
+    {
+        if ( line.size () < 159 ) fputs ( std::string ( 159 - line.size (), ' ' ).c_str (), out );
+        fprintf ( out, "\n%s\n", blank.c_str () );
+    }
+    fprintf ( out, "%s\n", std::string ( 79, '=' ).c_str () );
+
+    const size_t na = strlen ( alphabet );
+    std::string id;
+    for ( uint32_t r = 0; r < res.count; ++r )
+    {
+        const std::string & w = words[r];
+        id.resize ( w.size () );
+        for ( size_t i = 0; i < w.size (); ++i )
+        {
+            const char * at = w[i] ? ( const char * ) memchr ( alphabet, w[i], na ) : nullptr;
+            id[i] = at ? ( char ) ( '0' + ( at - alphabet ) ) : ( P.nb_gaps ? '-' : ( char ) ( '0' + na ) );
+        }
+        fprintf ( out, "%s %s %d\t%d\n", w.c_str (), id.c_str (), res.motifs[r].u, res.motifs[r].v );
+    }
+    fprintf ( out, "Nb models: %d\n", res.count );
+    fprintf ( out, "User time: %lf sec.\n", secs );
+}
+
 int main ( int argc, char ** argv )
 {
     Switches sw;
@@ -206,10 +283,30 @@ int main ( int argc, char ** argv )
         fprintf ( stderr, " Error: alphabet argument a should be `DNA' for nucleotide sequences or `PROT' for protein sequences or `USR' for sequences over a user-defined alphabet!\n" );
         return 1;
     }
-    if ( sw.background_in_filename || sw.un_in_filename || sw.un_out_filename || sw.smile_out_filename ||
-         sw.un_smile_out_filename )
+    /* option combinations (motex.cc:147-201) */
+    if ( ! sw.background_in_filename )
     {
-        fprintf ( stderr, " Error: the background, unmatched and SMILE modes (-b -u -U -I -S) are not part of motexGPU!\n" );
+        if ( sw.un_out_filename ) { fprintf ( stderr, " Error: `-u' option must be used with `-b' option!\n" ); return 1; }
+        if ( sw.un_smile_out_filename ) { fprintf ( stderr, " Error: `-U' option must be used with `-b' option!\n" ); return 1; }
+    }
+    else
+    {
+        if ( ! sw.un_out_filename ) { fprintf ( stderr, " Error: `-b' option must be used with `-u' option!\n" ); return 1; }
+        if ( sw.un_smile_out_filename && ! sw.smile_out_filename )
+        {
+            fprintf ( stderr, " Error: `-U' option must be used with `-S' option!\n" );
+            return 1;
+        }
+        if ( sw.un_in_filename ) { fprintf ( stderr, " Error: `-I' option cannot be used with `-b' option!\n" ); return 1; }
+    }
+    if ( sw.boxes_in_filename && sw.un_in_filename )
+    {
+        fprintf ( stderr, " Error: `-I' option cannot be used with `-s' option!\n" );
+        return 1;
+    }
+    if ( sw.background_in_filename || sw.un_in_filename )
+    {
+        fprintf ( stderr, " Error: the background and unmatched-motif modes (-b -u -U -I) are not part of motexGPU!\n" );
         return 1;
     }
 
@@ -284,42 +381,68 @@ int main ( int argc, char ** argv )
     }
     const unsigned num_seqs = ( unsigned ) seqs.size ();
 
-    FILE * out = fopen ( sw.output_filename, "w" );
-    if ( ! out ) { fprintf ( stderr, " Error: cannot open file!\n" ); return 1; }
-    write_header ( out, sw, P, num_seqs, end - start );
-    std::string word;
+    /* the printed words: box 0, then each further box after its gap, joined
+       by '_' (functions.cc:1191-1239); symbols past a sequence end read as NUL */
+    std::vector<std::string> words ( res.count );
+    std::vector<unsigned> S ( P.nb_gaps );
     for ( uint32_t r = 0; r < res.count; ++r )
     {
         const motex_motif & m = res.motifs[r];
         const std::string & s = seqs[m.seq];
-        const unsigned jj = m.pos + 1 - sw.l;
+        const size_t jj = m.pos + 1 - sw.l;
+        std::string & word = words[r];
         word.assign ( s, jj, sw.l );
         if ( P.nb_gaps )
         {
-            // boxes joined by '_', gaps left out (functions.cc:1191-1239)
-            unsigned offset = 0, ell = sw.l, rem = m.strct;
-            std::vector<unsigned> S ( P.nb_gaps );
+            unsigned rem = m.strct;
             for ( int g = ( int ) P.nb_gaps - 1; g >= 0; --g )
             {
                 unsigned span = P.gap_max[g] - P.gap_min[g] + 1;
                 S[g] = P.gap_min[g] + rem % span;
                 rem /= span;
             }
+            size_t offset = 0, ell = sw.l;
             for ( unsigned b = 1; b <= P.nb_gaps; ++b )
             {
                 offset += S[b - 1] + ell;
                 ell = P.blens[b - 1];
                 word.push_back ( '_' );
-                word.append ( s, jj + offset, ell );
+                for ( size_t q = 0; q < ell; ++q )
+                    word.push_back ( jj + offset + q < s.size () ? s[jj + offset + q] : '\0' );
             }
         }
-        fprintf ( out, "%s %d %d %lf %d\n", word.c_str (), m.u, num_seqs, ( double ) m.u / num_seqs, m.v );
     }
-    if ( P.nb_gaps )
-        fprintf ( out, "\n#A total of %d valid structured motifs were extracted.\n\n", res.count );
+
+    /* a file that cannot be opened is reported and skipped; the exit status
+       stays 0, as the reference ignores its writers' status (motex.cc:836-866) */
+    FILE * out = fopen ( sw.output_filename, "w" );
+    if ( ! out ) fprintf ( stderr, " Error: cannot open file!\n" );
     else
-        fprintf ( out, "\n#A total of %d valid motifs were extracted.\n\n", res.count );
-    if ( fclose ( out ) ) { fprintf ( stderr, " Error: file close error!\n" ); return 1; }
+    {
+        write_header ( out, sw, P, num_seqs, end - start );
+        for ( uint32_t r = 0; r < res.count; ++r )
+        {
+            const motex_motif & m = res.motifs[r];
+            fprintf ( out, "%s %d %d %lf %d\n", words[r].c_str (), m.u, num_seqs, ( double ) m.u / num_seqs, m.v );
+        }
+        if ( P.nb_gaps )
+            fprintf ( out, "\n#A total of %d valid structured motifs were extracted.\n\n", res.count );
+        else
+            fprintf ( out, "\n#A total of %d valid motifs were extracted.\n\n", res.count );
+        if ( fclose ( out ) ) fprintf ( stderr, " Error: file close error!\n" );
+    }
+    if ( sw.smile_out_filename )
+    {
+        FILE * so = fopen ( sw.smile_out_filename, "w" );
+        if ( ! so ) fprintf ( stderr, " Error: cannot open file!\n" );
+        else
+        {
+            unsigned total_length = 0;
+            for ( const std::string & q : seqs ) total_length += ( unsigned ) q.size ();
+            write_smile ( so, sw, P, num_seqs, total_length, alphabet, words, res, end - start );
+            if ( fclose ( so ) ) fprintf ( stderr, " Error: file close error!\n" );
+        }
+    }
 
     const char * mpath = getenv ( "MOTEX_METRICS" );
     if ( mpath && *mpath )

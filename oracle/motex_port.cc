@@ -16,11 +16,15 @@
  *   structured extraction   functions.cc:564-705 (HD), 773-915 (ED)
  *   header                  functions.cc:1010-1068
  *   writers                 functions.cc:1073-1142, 1147-1260
+ *   SMILE-like file (-S)    functions.cc:1262-1345, 1368-1461, 1463-1591
  *
  * The DP primitives are motex_core.h (restated libFLASM semantics, pinned
- * against the shipped library by flasm_difftest.cc).  The statistics /
- * SMILE / background modes (-b -u -U -I -S) are outside the hot path and are
- * rejected with an error.
+ * against the shipped library by flasm_difftest.cc).  The background and
+ * unmatched-motif modes follow the reference built without MPFR (binomial.cc
+ * long double flavour), which is what oracle/build_ref.sh compiles:
+ *   -b -u [-S -U]           functions.cc:1613-2238 (-o/-u), 2241-2748 (SMILE)
+ *   -I                      motex.cc:883-1137, functions.cc:2750-2829
+ *   binomial tail           binomial.cc:78-103
  *
  * Built twice: as the CLI binary (main) and, with -DMOTEX_PORT_LIB, as a
  * shared library exposing oracle_extract_pair() and oracle_word_uv() for
@@ -33,12 +37,15 @@
 #include <string.h>
 #include <ctype.h>
 #include <getopt.h>
+#include <math.h>
 #include <time.h>
 #include <sys/time.h>
 #include <stdint.h>
 #include <string>
 #include <vector>
+#include <unordered_map>
 #include <unordered_set>
+#include <algorithm>
 #ifdef _OPENMP
 #include <omp.h>
 #endif
@@ -429,6 +436,338 @@ static bool passes ( const Switch & sw, unsigned u, unsigned v, unsigned num_seq
     return r >= sw.q && v >= sw.n && r <= sw.Q && v <= sw.N;
 }
 
+struct Printed
+{
+    std::string key;
+    unsigned u, v;
+};
+
+/* functions.cc:1262-1345: the SMILE-like header */
+static void write_smile_header ( FILE * out, const Switch & sw, const Params & P, const std::vector<unsigned> & gmin,
+                                 const std::vector<unsigned> & gmax, unsigned num_seqs, unsigned total_length,
+                                 const char * alphabet )
+{
+    char head[1024];
+    int at;
+    int abs_q = ( int ) ceil ( ( double ) ( ( double ) sw.q * num_seqs ) / ( double ) 100 );
+    if ( P.nb_boxes == 1 )
+        at = snprintf ( head, sizeof head, "%%%%%% 1 %d/%d %d %d %d %d alphabet %s$", abs_q, num_seqs, total_length,
+                        sw.l, sw.l, sw.e, alphabet );
+    else
+    {
+        unsigned tot = sw.l, errs = sw.e;
+        for ( unsigned b = 0; b < P.nb_gaps; ++b ) { tot += P.blens[b]; errs += P.berrs[b]; }
+        at = snprintf ( head, sizeof head, "%%%%%% %d %d/%d %d %d %d %d %d %d %d ", P.nb_boxes, abs_q, num_seqs,
+                        total_length, tot, tot, errs, sw.l, sw.l, sw.e );
+        for ( unsigned b = 0; b < P.nb_gaps; ++b )
+            at += snprintf ( head + at, sizeof head - at, "%d %d %d %d %d ", gmin[b], gmax[b], P.blens[b], P.blens[b], P.berrs[b] );
+        at += snprintf ( head + at, sizeof head - at, "alphabet %s$", alphabet );
+    }
+    fprintf ( out, "%s", head );
+    int width = 0, blank_lines = 0;
+    if ( ! strcmp ( sw.alphabet, "DNA" ) ) { width = 79; blank_lines = 2; }
+    if ( ! strcmp ( sw.alphabet, "PROT" ) ) { width = 159; blank_lines = 1; }
+    if ( width )
+    {
+        for ( int i = at; i < width; ++i ) fputc ( ' ', out );
+        fputc ( '\n', out );
+        for ( int b = 0; b < blank_lines; ++b ) fprintf ( out, "%79s\n", "" );
+    }
+    for ( int i = 0; i < 79; ++i ) fputc ( '=', out );
+    fputc ( '\n', out );
+}
+
+/* functions.cc:1368-1461, 1463-1591: "key id u<TAB>v", id = '0' + rank of
+   each symbol in the alphabet string ('-' for a separator) */
+static std::string smile_line ( const Params & P, const char * alphabet, const Printed & p )
+{
+    const unsigned na = ( unsigned ) strlen ( alphabet );
+    std::string id;
+    for ( char c : p.key )
+    {
+        unsigned r = 0;
+        while ( r < na && alphabet[r] != c ) ++r;
+        id.push_back ( r < na ? ( char ) ( '0' + r ) : ( P.nb_gaps ? '-' : ( char ) ( '0' + r ) ) );
+    }
+    char tail[64];
+    snprintf ( tail, sizeof tail, " %d\t%d\n", p.u, p.v );
+    return std::string ( p.key.c_str () ) + " " + id + tail;
+}
+
+static void write_smile_lines ( FILE * out, const Params & P, const char * alphabet, const std::vector<Printed> & printed )
+{
+    for ( const Printed & p : printed ) fputs ( smile_line ( P, alphabet, p ).c_str (), out );
+}
+
+/* binomial.cc:78-103, the long double flavour (built without MPFR):
+   a[i] = i!, and P(X < x) for X ~ Bin(N, p), 0 when p >= 1 */
+static std::vector<long double> fact_table ( int n )
+{
+    std::vector<long double> a ( ( size_t ) n + 1 );
+    a[0] = 1;
+    for ( int i = 1; i <= n; ++i ) a[i] = a[i - 1] * i;
+    return a;
+}
+
+static long double binomial_cdf_below ( int x, int N, long double p, const long double * LUT )
+{
+    long double prob = 0., pr = 0.;
+    if ( p >= 1.0 ) return 0.;
+    for ( int i = 0; i < x; ++i )
+    {
+        pr = ( LUT[N] / LUT[i] ) / LUT[N - i] * powl ( p, ( long double ) i ) * powl ( 1. - p, ( long double ) ( N - i ) );
+        prob += pr;
+        if ( x > N ) break;
+    }
+    return prob;
+}
+
+/* The header lines the background reader takes (functions.cc:1683-1712):
+   line 6 "# For N input sequences" and line 8 "#     q = Q"; then one motif
+   per line up to the next blank line: key (its first klen symbols), u, n,
+   r, v.  A repeated key keeps its last entry. */
+struct BgEntry
+{
+    unsigned u, n, v;
+    double r;
+};
+
+static bool read_background ( const char * path, unsigned klen, int * bsize, int * bquorum,
+                              std::unordered_map<std::string, int> & index, std::vector<BgEntry> & entries )
+{
+    FILE * in = fopen ( path, "r" );
+    if ( ! in ) return false;
+    char line[512];
+    unsigned line_num = 0;
+    std::string size_s, quorum_s;
+    while ( fgets ( line, sizeof line, in ) && line[0] != '\n' )
+    {
+        ++line_num;
+        if ( line_num == 6 || line_num == 8 )
+        {
+            char * save = nullptr;
+            char * tok = strtok_r ( line, " ", &save );
+            tok = tok ? strtok_r ( nullptr, " ", &save ) : nullptr;
+            tok = tok ? strtok_r ( nullptr, " ", &save ) : nullptr;
+            if ( line_num == 8 ) tok = tok ? strtok_r ( nullptr, "\n", &save ) : nullptr;
+            ( line_num == 6 ? size_s : quorum_s ) = tok ? tok : "";
+        }
+    }
+    *bsize = atoi ( size_s.c_str () );
+    *bquorum = atoi ( quorum_s.c_str () );
+    while ( fgets ( line, sizeof line, in ) && line[0] != '\n' )
+    {
+        char * save = nullptr;
+        char * tok = strtok_r ( line, " ", &save );
+        const char * f[4] = { nullptr, nullptr, nullptr, nullptr };
+        for ( int q = 0; q < 4 && tok; ++q ) f[q] = strtok_r ( nullptr, " ", &save );
+        if ( ! tok ) continue;
+        std::string key ( tok, strnlen ( tok, klen ) );
+        BgEntry b { ( unsigned ) atoi ( f[0] ? f[0] : "0" ), ( unsigned ) atoi ( f[1] ? f[1] : "0" ),
+                    ( unsigned ) atoi ( f[3] ? f[3] : "0" ), atof ( f[2] ? f[2] : "0" ) };
+        index[key] = ( int ) entries.size ();
+        entries.push_back ( b );
+    }
+    fclose ( in );
+    return true;
+}
+
+/* functions.cc:1613-1895 (plain) and 1900-2238 (structured), long double
+   flavour: every printed motif either matches an unused background entry
+   (p-value from binomial_cdf_below(u, num_seqs, that entry's u)) or is
+   unmatched (p = Q / N of the background header) and also goes to -u. */
+static bool write_background ( const Switch & sw, const Params & P, const std::vector<unsigned> & gmin,
+                               const std::vector<unsigned> & gmax, unsigned num_seqs,
+                               const std::vector<Printed> & printed, double exectime, int procs )
+{
+    FILE * out = fopen ( sw.output_filename, "w" );
+    if ( ! out ) { fprintf ( stderr, " Error: cannot open file!\n" ); return true; }
+    write_header ( out, sw, P, gmin, gmax, num_seqs, exectime, procs );
+    FILE * un = fopen ( sw.un_out_filename, "w" );
+    if ( ! un ) { fprintf ( stderr, " Error: cannot open file!\n" ); fclose ( out ); return true; }
+    write_header ( un, sw, P, gmin, gmax, num_seqs, exectime, procs );
+    unsigned klen = sw.l;
+    for ( unsigned b = 0; b < P.nb_gaps; ++b ) klen += P.blens[b] + 1;
+    int bsize = 0, bquorum = 0;
+    std::unordered_map<std::string, int> index;
+    std::vector<BgEntry> bg;
+    if ( ! read_background ( sw.background_in_filename, klen, &bsize, &bquorum, index, bg ) )
+    {
+        fprintf ( stderr, " Error: cannot open file!\n" );
+        fclose ( out );
+        fclose ( un );
+        return true;
+    }
+    if ( ! ( bsize > 0 && bquorum > 0 ) )
+    {
+        /* the reference asserts here (functions.cc:1714) and aborts */
+        fprintf ( stderr, " Error: background file %s gives no sequence count or no quorum!\n", sw.background_in_filename );
+        fclose ( out );
+        fclose ( un );
+        return false;
+    }
+    std::vector<long double> LUT = fact_table ( ( int ) num_seqs );
+    unsigned pvalid = 0, uvalid = 0;
+    for ( const Printed & p : printed )
+    {
+        const double r = ( double ) p.u / num_seqs;
+        auto it = index.find ( p.key );
+        if ( it == index.end () || it->second < 0 )
+        {
+            long double cdf = binomial_cdf_below ( ( int ) p.u, ( int ) num_seqs, ( long double ) bquorum / bsize, LUT.data () );
+            fprintf ( out, "%s %d %d %lf %d %d %d %Le\n", p.key.c_str (), p.u, num_seqs, r, p.v, 0, 0, 1. - cdf );
+            fprintf ( un, "%s %d %d %lf %d\n", p.key.c_str (), p.u, num_seqs, r, p.v );
+            uvalid++;
+        }
+        else
+        {
+            const BgEntry & b = bg[it->second];
+            long double cdf = binomial_cdf_below ( ( int ) p.u, ( int ) num_seqs, ( long double ) b.u, LUT.data () );
+            fprintf ( out, "%s %d %d %lf %d %lf %d %Le\n", p.key.c_str (), p.u, num_seqs, r, p.v, b.r, b.v, 1. - cdf );
+            pvalid++;
+        }
+        index[p.key] = -1;
+    }
+    fprintf ( out, "\n#A total of %d background motifs were read.\n", ( int ) bg.size () );
+    fprintf ( out, "#A total of %d valid motifs were extracted:\n", pvalid + uvalid );
+    fprintf ( out, "#  %d of them were matched with background motifs\n", pvalid );
+    fprintf ( out, "#  %d of them were not matched with any background motif.\n\n", uvalid );
+    fprintf ( un, "\n#A total of %d background motifs were read.\n", ( int ) bg.size () );
+    fprintf ( un, "#A total of %d valid motifs were extracted:\n", pvalid + uvalid );
+    fprintf ( un, "#  %d of them were not matched with any background motif.\n\n", uvalid );
+    fclose ( out );
+    fclose ( un );
+    return true;
+}
+
+/* functions.cc:2241-2468 (plain) and 2469-2748 (structured): -S gets every
+   printed motif, -U the unmatched ones, both in the SMILE-like format */
+static void write_background_smile ( const Switch & sw, const Params & P, const std::vector<unsigned> & gmin,
+                                     const std::vector<unsigned> & gmax, unsigned num_seqs, unsigned total_length,
+                                     const char * alphabet, const std::vector<Printed> & printed, double exectime )
+{
+    FILE * un = fopen ( sw.un_smile_out_filename, "w" );
+    if ( ! un ) { fprintf ( stderr, " Error: cannot open file %s!\n", sw.un_smile_out_filename ); return; }
+    write_smile_header ( un, sw, P, gmin, gmax, num_seqs, total_length, alphabet );
+    FILE * out = fopen ( sw.smile_out_filename, "w" );
+    if ( ! out ) { fprintf ( stderr, " Error: cannot open file %s!\n", sw.smile_out_filename ); fclose ( un ); return; }
+    write_smile_header ( out, sw, P, gmin, gmax, num_seqs, total_length, alphabet );
+    unsigned klen = sw.l;
+    for ( unsigned b = 0; b < P.nb_gaps; ++b ) klen += P.blens[b] + 1;
+    int bsize = 0, bquorum = 0;
+    std::unordered_map<std::string, int> index;
+    std::vector<BgEntry> bg;
+    if ( ! read_background ( sw.background_in_filename, klen, &bsize, &bquorum, index, bg ) )
+    {
+        fprintf ( stderr, " Error: cannot open file %s!\n", sw.background_in_filename );
+        fclose ( out );
+        fclose ( un );
+        return;
+    }
+    unsigned pvalid = 0, uvalid = 0;
+    for ( const Printed & p : printed )
+    {
+        auto it = index.find ( p.key );
+        const std::string line = smile_line ( P, alphabet, p );
+        if ( it == index.end () || it->second < 0 )
+        {
+            fputs ( line.c_str (), un );
+            uvalid++;
+        }
+        else
+            pvalid++;
+        fputs ( line.c_str (), out );
+        index[p.key] = -1;
+    }
+    fprintf ( out, "Nb models: %d\n", pvalid + uvalid );
+    fprintf ( out, "User time: %lf sec.\n", exectime );
+    fprintf ( un, "Nb models: %d\n", uvalid );
+    fprintf ( un, "User time: %lf sec.\n", exectime );
+    fclose ( un );
+    fclose ( out );
+}
+
+/* motex.cc:883-1137 (-I): the motif file's lines after its first blank
+   line, up to the next one, are "motif u n r v"; each motif (all of its
+   factors) is searched in every sequence at least total_mot_length long,
+   and write_motifs_fore (functions.cc:2750-2829) prints the entry of its
+   last factor with p-value 1 - P(X < u_file), X ~ Bin(n_file, u / N). */
+static int foreground ( const Switch & sw, const Params & P, const std::vector<std::string> & seqs,
+                        unsigned total_mot_length, int procs )
+{
+    FILE * in = fopen ( sw.un_in_filename, "r" );
+    if ( ! in ) { fprintf ( stderr, " Error: Cannot open file %s!\n", sw.un_in_filename ); return 1; }
+    char line[512];
+    while ( fgets ( line, sizeof line, in ) && line[0] != '\n' );
+    std::vector<std::string> fseqs;
+    std::vector<BgEntry> fdata;
+    while ( fgets ( line, sizeof line, in ) && line[0] != '\n' )
+    {
+        char * save = nullptr;
+        char * tok = strtok_r ( line, " ", &save );
+        const char * f[4] = { nullptr, nullptr, nullptr, nullptr };
+        for ( int q = 0; q < 4 && tok; ++q ) f[q] = strtok_r ( nullptr, " ", &save );
+        if ( ! tok || ! f[3] )
+        {
+            fprintf ( stderr, " Error: file %s is not in the correct format!\n", sw.un_in_filename );
+            fclose ( in );
+            return 1;
+        }
+        fseqs.push_back ( tok );
+        fdata.push_back ( { ( unsigned ) atoi ( f[0] ), ( unsigned ) atoi ( f[1] ), ( unsigned ) atoi ( f[3] ), atof ( f[2] ) } );
+    }
+    fclose ( in );
+
+    const unsigned num_seqs = ( unsigned ) seqs.size (), nf = ( unsigned ) fseqs.size ();
+    std::vector<std::string> all ( fseqs );
+    all.insert ( all.end (), seqs.begin (), seqs.end () );
+    Coded C = encode ( all );
+    std::vector<std::vector<unsigned>> U ( nf ), V ( nf );
+    double start = gettime ();
+    #pragma omp parallel for schedule(dynamic, 1)
+    for ( unsigned i = 0; i < nf; ++i )
+    {
+        const std::vector<unsigned char> & x = C.seq[i];
+        const unsigned m = ( unsigned ) x.size ();
+        U[i].assign ( m, 0 );
+        V[i].assign ( m, 0 );
+        if ( m < P.l ) continue;                      /* no factor (the reference's flasm call is undefined) */
+        std::vector<uint64_t> peq;
+        if ( P.d == 1 ) build_peq ( x, P.l, C.sigma, peq );
+        std::vector<unsigned char> occ;
+        for ( unsigned j = 0; j < num_seqs; ++j )
+        {
+            const std::vector<unsigned char> & t = C.seq[nf + j];
+            if ( total_mot_length > t.size () ) continue;
+            extract_plain ( P, x, t, P.d == 1 ? &peq : nullptr, C.sigma, U[i].data (), V[i].data (), occ );
+        }
+    }
+    double end = gettime ();
+
+    FILE * out = fopen ( sw.output_filename, "w" );
+    if ( ! out ) { fprintf ( stderr, " Error: cannot open file!\n" ); return 0; }
+    std::vector<unsigned> none;
+    write_header ( out, sw, P, none, none, num_seqs, end - start, procs );
+    unsigned maxn = num_seqs;
+    for ( const BgEntry & f : fdata ) maxn = std::max ( maxn, f.n );
+    std::vector<long double> LUT = fact_table ( ( int ) maxn );
+    unsigned valid = 0;
+    for ( unsigned i = 0; i < nf; ++i )
+    {
+        const unsigned m = ( unsigned ) fseqs[i].size ();
+        if ( m == 0 ) continue;
+        const unsigned u = U[i][m - 1], v = V[i][m - 1];
+        if ( ! passes ( sw, u, v, num_seqs ) ) continue;
+        long double cdf = binomial_cdf_below ( ( int ) fdata[i].u, ( int ) fdata[i].n, ( long double ) u / num_seqs, LUT.data () );
+        fprintf ( out, "%s %d %d %lf %d %lf %d %Le\n", fseqs[i].c_str (), fdata[i].u, fdata[i].n, fdata[i].r, fdata[i].v,
+                  ( double ) u / num_seqs, v, 1. - cdf );
+        valid++;
+    }
+    fprintf ( out, "\n#A total of %d valid motifs were extracted.\n\n", valid );
+    fclose ( out );
+    return 0;
+}
+
 int main ( int argc, char ** argv )
 {
     Switch sw;
@@ -451,11 +790,13 @@ int main ( int argc, char ** argv )
         fprintf ( stderr, " Error: alphabet argument a should be `DNA' for nucleotide sequences or `PROT' for protein sequences or `USR' for sequences over a user-defined alphabet!\n" );
         return 1;
     }
-    if ( sw.background_in_filename || sw.un_in_filename || sw.un_out_filename || sw.smile_out_filename || sw.un_smile_out_filename )
-    {
-        fprintf ( stderr, " Error: -b/-u/-U/-I/-S are not part of the extraction path restated here!\n" );
-        return 1;
-    }
+    /* motex.cc:147-201 */
+    if ( ! sw.background_in_filename && sw.un_out_filename ) { fprintf ( stderr, " Error: `-u' option must be used with `-b' option!\n" ); return 1; }
+    if ( ! sw.background_in_filename && sw.un_smile_out_filename ) { fprintf ( stderr, " Error: `-U' option must be used with `-b' option!\n" ); return 1; }
+    if ( sw.background_in_filename && ! sw.un_out_filename ) { fprintf ( stderr, " Error: `-b' option must be used with `-u' option!\n" ); return 1; }
+    if ( sw.background_in_filename && sw.un_smile_out_filename && ! sw.smile_out_filename ) { fprintf ( stderr, " Error: `-U' option must be used with `-S' option!\n" ); return 1; }
+    if ( sw.background_in_filename && sw.un_in_filename ) { fprintf ( stderr, " Error: `-I' option cannot be used with `-b' option!\n" ); return 1; }
+    if ( sw.boxes_in_filename && sw.un_in_filename ) { fprintf ( stderr, " Error: `-I' option cannot be used with `-s' option!\n" ); return 1; }
 
     /* motex.cc:225-300 FASTA reader */
     FILE * in = fopen ( sw.input_filename, "r" );
@@ -532,17 +873,18 @@ int main ( int argc, char ** argv )
     threads = 1;
 #endif
     const unsigned num_seqs = ( unsigned ) seqs.size ();
+    if ( sw.un_in_filename )
+        return foreground ( sw, P, seqs, total_mot_length, ( int ) threads );
     Coded C = encode ( seqs );
     std::vector<std::vector<unsigned>> U, V;
     double start = gettime ();
     all_pairs ( P, C, total_mot_length, U, V, sw.input_filename );
     double end = gettime ();
 
-    FILE * out = fopen ( sw.output_filename, "w" );
-    if ( ! out ) { fprintf ( stderr, " Error: cannot open file!\n" ); return 1; }
-    write_header ( out, sw, P, gmin, gmax, num_seqs, end - start, ( int ) threads );
+    /* the motifs every writer visits: first passing occurrence of each key,
+       (sequence, end position[, structure]) order */
     std::unordered_set<std::string> seen;
-    unsigned valid = 0;
+    std::vector<Printed> printed;
     if ( P.nb_gaps == 0 )
     {
         /* functions.cc:1073-1142 */
@@ -553,14 +895,9 @@ int main ( int argc, char ** argv )
             {
                 if ( ! passes ( sw, U[s][j], V[s][j], num_seqs ) ) continue;
                 std::string w = seqs[s].substr ( j - sw.l + 1, sw.l );
-                if ( seen.insert ( w ).second )
-                {
-                    fprintf ( out, "%s %d %d %lf %d\n", w.c_str (), U[s][j], num_seqs, ( double ) U[s][j] / num_seqs, V[s][j] );
-                    valid++;
-                }
+                if ( seen.insert ( w ).second ) printed.push_back ( { w, U[s][j], V[s][j] } );
             }
         }
-        fprintf ( out, "\n#A total of %d valid motifs were extracted.\n\n", valid );
     }
     else
     {
@@ -586,16 +923,42 @@ int main ( int argc, char ** argv )
                             key.push_back ( at < m ? seqs[s][at] : '\0' );
                         }
                     }
-                    if ( seen.insert ( key ).second )
-                    {
-                        fprintf ( out, "%s %d %d %lf %d\n", key.c_str (), U[s][idx], num_seqs, ( double ) U[s][idx] / num_seqs, V[s][idx] );
-                        valid++;
-                    }
+                    if ( seen.insert ( key ).second ) printed.push_back ( { key, U[s][idx], V[s][idx] } );
                 }
         }
-        fprintf ( out, "\n#A total of %d valid structured motifs were extracted.\n\n", valid );
     }
+    unsigned total_length = 0;
+    for ( const std::string & q : seqs ) total_length += ( unsigned ) q.size ();
+
+    if ( sw.background_in_filename )
+    {
+        /* motex.cc:844-849, 860-865: the -o/-u pair, then the SMILE pair only with -U */
+        if ( ! write_background ( sw, P, gmin, gmax, num_seqs, printed, end - start, ( int ) threads ) ) return 1;
+        if ( sw.un_smile_out_filename )
+            write_background_smile ( sw, P, gmin, gmax, num_seqs, total_length, alphabet, printed, end - start );
+        return 0;
+    }
+
+    FILE * out = fopen ( sw.output_filename, "w" );
+    if ( ! out ) { fprintf ( stderr, " Error: cannot open file!\n" ); return 1; }
+    write_header ( out, sw, P, gmin, gmax, num_seqs, end - start, ( int ) threads );
+    for ( const Printed & pr : printed )
+        fprintf ( out, "%s %d %d %lf %d\n", pr.key.c_str (), pr.u, num_seqs, ( double ) pr.u / num_seqs, pr.v );
+    if ( P.nb_gaps == 0 )
+        fprintf ( out, "\n#A total of %d valid motifs were extracted.\n\n", ( int ) printed.size () );
+    else
+        fprintf ( out, "\n#A total of %d valid structured motifs were extracted.\n\n", ( int ) printed.size () );
     if ( fclose ( out ) ) { fprintf ( stderr, " Error: file close error!\n" ); return 1; }
+    if ( sw.smile_out_filename )
+    {
+        FILE * so = fopen ( sw.smile_out_filename, "w" );
+        if ( ! so ) { fprintf ( stderr, " Error: cannot open file!\n" ); return 0; }
+        write_smile_header ( so, sw, P, gmin, gmax, num_seqs, total_length, alphabet );
+        write_smile_lines ( so, P, alphabet, printed );
+        fprintf ( so, "Nb models: %d\n", ( int ) printed.size () );
+        fprintf ( so, "User time: %lf sec.\n", end - start );
+        fclose ( so );
+    }
     return 0;
 }
 

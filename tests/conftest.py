@@ -49,4 +49,4 @@ def golden_cases():
 
 def strip_volatile(text: str) -> str:
     return "".join(l for l in text.splitlines(True)
-                   if not l.startswith("# Rundate:") and not l.startswith("# Run on "))
+                   if not l.startswith(("# Rundate:", "# Run on ", "User time:")))

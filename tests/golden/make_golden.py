@@ -7,8 +7,11 @@ with the libflasm.so shipped in the reference (x86-64 only).  The restated
 oracle (oracle/_build/motex_port) is run on every case as well and must give
 the identical file; a mismatch aborts the script.
 
+Cases listed in SMILE_CASES also run with ``-S out.smile`` and store the
+SMILE-like file as expected.smile.
+
 The two non-deterministic header lines (``# Rundate:`` and ``# Run on ...``)
-are removed from stored outputs.  Cases run with relative paths (in.fa,
+and the SMILE file's ``User time:`` line are removed from stored outputs.  Cases run with relative paths (in.fa,
 in.boxes, out.motex) from the case directory, so the header's file lines are
 reproducible.
 
@@ -37,19 +40,28 @@ REF = os.path.join(ROOT, "oracle", "_ref")
 PORT = os.path.join(ROOT, "oracle", "_build", "motex_port")
 
 
+SMILE_CASES = {"c1_dna_hd_64x500", "prot_hd_20seq", "prot_ed_20seq", "usr_hd", "dna_with_N_ed",
+               "quorum_boundary_q29", "short_seqs_ed", "struct_planted_hd", "struct_planted_ed",
+               "struct2_planted_ed", "struct_long_gap_hd"}
+
+
 def strip_volatile(text: str) -> str:
     return "".join(l for l in text.splitlines(True)
-                   if not l.startswith("# Rundate:") and not l.startswith("# Run on "))
+                   if not l.startswith(("# Rundate:", "# Run on ", "User time:")))
 
 
 def run_cli(binary, args, cwd):
+    """Returns (rc, main output, SMILE output or None)."""
     p = subprocess.run([binary] + args, cwd=cwd, capture_output=True, text=True)
-    out = None
-    if os.path.exists(os.path.join(cwd, "out.motex")):
-        with open(os.path.join(cwd, "out.motex")) as f:
-            out = strip_volatile(f.read())
-        os.remove(os.path.join(cwd, "out.motex"))
-    return p.returncode, out
+    outs = []
+    for name in ("out.motex", "out.smile"):
+        path = os.path.join(cwd, name)
+        outs.append(None)
+        if os.path.exists(path):
+            with open(path) as f:
+                outs[-1] = strip_volatile(f.read())
+            os.remove(path)
+    return p.returncode, outs[0], outs[1]
 
 
 # --------------------------------------------------------------- case inputs
@@ -225,20 +237,25 @@ def main():
         if w.boxes:
             W.write_boxes(os.path.join(d, "in.boxes"), w.boxes)
         args = w.cli("in.fa", "out.motex", "in.boxes" if w.boxes else None) + extra
+        if name in SMILE_CASES:
+            args += ["-S", "out.smile"]
         big = w.total_len ** 2 * (len(w.boxes) + 1) > 3e8
         ref_bin = os.path.join(REF, "motexOMP" if big else "motexCPU")
         ref_args = args + (["-t", str(os.cpu_count())] if big else [])
         with tempfile.TemporaryDirectory() as tmp:
             for f in os.listdir(d):
                 shutil.copy(os.path.join(d, f), tmp)
-            rc, ref_out = run_cli(ref_bin, ref_args, tmp)
-            rc2, port_out = run_cli(PORT, args + ["-t", str(os.cpu_count())], tmp)
-        if rc != 0 or ref_out is None:
+            rc, ref_out, ref_smile = run_cli(ref_bin, ref_args, tmp)
+            rc2, port_out, port_smile = run_cli(PORT, args + ["-t", str(os.cpu_count())], tmp)
+        if rc != 0 or ref_out is None or (name in SMILE_CASES and ref_smile is None):
             sys.exit(f"make_golden: reference failed on {name} (rc={rc})")
-        if rc2 != rc or port_out != ref_out:
+        if rc2 != rc or port_out != ref_out or port_smile != ref_smile:
             sys.exit(f"make_golden: oracle/_build/motex_port disagrees with the reference on {name}")
         with open(os.path.join(d, "expected.motex"), "w") as f:
             f.write(ref_out)
+        if ref_smile is not None:
+            with open(os.path.join(d, "expected.smile"), "w") as f:
+                f.write(ref_smile)
         with open(os.path.join(d, "case.json"), "w") as f:
             json.dump({"args": args, "reference": os.path.basename(ref_bin),
                        "motifs": ref_out.count("\n") - ref_out.count("#") - 3}, f, indent=1)

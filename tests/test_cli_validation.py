@@ -44,3 +44,39 @@ def test_rejections_match_oracle(native_built, oracle_port, name, args, fasta):
 def test_missing_mandatory_switches(native_built):
     rc, out, err = run_cli(native_built.CLI_PATH, None, ["-a", "DNA", "-i", "in.fa"], files={"in.fa": FA})
     assert rc == 1 and out is None
+
+
+@pytest.mark.parametrize("boxes", ["", "x\n", "1\n5\n", "1\n5\n15\n10\n"], ids=["empty", "not_int", "short", "no_err"])
+def test_bad_boxes_file(native_built, oracle_port, boxes):
+    args = BASE + ["-s", "in.boxes"]
+    files = {"in.fa": FA, "in.boxes": boxes}
+    g = run_cli(native_built.CLI_PATH, None, args, files=files)
+    o = run_cli(oracle_port, None, args, files=files)
+    assert g[0] == o[0] == 1
+    assert g[2] == o[2]
+
+
+COMBOS = [
+    ("u_without_b", ["-u", "un.txt"]),
+    ("U_without_b", ["-U", "un.smile"]),
+    ("b_without_u", ["-b", "bg.motex"]),
+    ("b_U_without_S", ["-b", "bg.motex", "-u", "un.txt", "-U", "un.smile"]),
+    ("b_with_I", ["-b", "bg.motex", "-u", "un.txt", "-I", "un.in"]),
+    ("s_with_I", ["-s", "in.boxes", "-I", "un.in"]),
+]
+
+
+@pytest.mark.parametrize("name,extra", COMBOS, ids=[c[0] for c in COMBOS])
+def test_option_combinations_match_oracle(native_built, oracle_port, name, extra):
+    """The reference's checks of -b/-u/-U/-S/-I/-s combinations (motex.cc:147-201)."""
+    files = {"in.fa": FA, "in.boxes": "1\n1\n2\n3\n0\n"}
+    g = run_cli(native_built.CLI_PATH, None, BASE + extra, files=files)
+    o = run_cli(oracle_port, None, BASE + extra, files=files)
+    assert g[0] == o[0] == 1
+    assert g[2] == o[2] and "Error" in g[2]
+
+
+@pytest.mark.parametrize("extra", [["-b", "bg.motex", "-u", "un.txt"], ["-I", "un.in"]], ids=["background", "unmatched_in"])
+def test_background_modes_rejected(native_built, extra):
+    rc, out, err = run_cli(native_built.CLI_PATH, None, BASE + extra, files={"in.fa": FA})
+    assert rc == 1 and out is None and "not part of motexGPU" in err

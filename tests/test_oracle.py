@@ -15,7 +15,7 @@ import subprocess
 import pytest
 
 from conftest import ORACLE_DIR, PORT_LIB, ROOT, golden_cases
-from helpers import load_case, run_cli
+from helpers import expected_smile, load_case, read_smile, run_cli
 
 REFERENCE = "/root/reference"
 
@@ -28,12 +28,24 @@ def test_port_matches_reference_golden(oracle_port, name):
     assert out == expected
 
 
+@pytest.mark.parametrize("name", [n for n in golden_cases() if expected_smile(n) is not None])
+def test_port_smile_matches_reference_golden(oracle_port, name):
+    """-S: the SMILE-like file (functions.cc:1262-1591) of the reference itself."""
+    d, args, expected = load_case(name)
+    rc, out, smile, err = read_smile(d, oracle_port, args, extra=["-t", "4"])
+    assert rc == 0, err
+    assert out == expected
+    assert smile == expected_smile(name)
+
+
 def test_golden_set_is_complete():
     names = set(golden_cases())
     for needed in ("c1_dna_hd_64x500", "dna_ed_24seq", "prot_hd_20seq", "prot_ed_20seq", "struct_planted_hd",
                    "struct_planted_ed", "quorum_boundary_q29", "dna_with_N_ed", "short_seqs_ed",
                    "long_factor_k70_ed", "q0_n0_all_words", "caps_Q60_n2_N40"):
         assert needed in names
+    smile = {n for n in names if expected_smile(n) is not None}
+    assert {"prot_hd_20seq", "usr_hd", "struct_planted_hd", "struct2_planted_ed"} <= smile
 
 
 def _difftest_binary():

@@ -226,6 +226,24 @@ int motex_gpu_extract_pair ( motex_ctx * ctx, const motex_params * prm,
                              const char * p, uint32_t m, const char * t, uint32_t n,
                              uint32_t * u, uint32_t * v );
 
+/*
+ * Word search: the counting loop of the reference's -I mode
+ * (motex.cc:938-1000, which calls motifs_extraction_hd/_ed with each motif
+ * read from the -I file as the pattern and every input sequence as the
+ * text; write_motifs_fore, functions.cc:2750-2829, then reads the entry of
+ * the motif's last factor).  For word i, u[i] = the number of sequences
+ * holding its last l symbols within e errors (distance d) at least once,
+ * v[i] = the number of such occurrences over all sequences.  Sequences
+ * shorter than l are skipped (motex.cc:977-982).  Words shorter than l get
+ * u = v = 0.  u and v are overwritten (nwords entries each).  Plain motifs
+ * only (nb_gaps = 0): the reference refuses -I with -s.  One GPU job: all
+ * words against all sequences in one DP launch sequence.
+ */
+int motex_gpu_search ( motex_ctx * ctx, const motex_params * prm,
+                       const char * const * words, const uint32_t * wlens, uint32_t nwords,
+                       const char * const * seqs, const uint32_t * lens, uint32_t nseq,
+                       uint32_t * u, uint32_t * v );
+
 /* Error reporting. */
 const char * motex_gpu_strerror ( int code );
 const char * motex_gpu_last_error ( void );

@@ -431,7 +431,7 @@ __global__ void k_wplanes_all ( const uint8_t * __restrict__ codes, uint32_t tot
 // Row bookkeeping of the pattern side: row_ok = box 0 may end here (sequence
 // long enough, full box inside it), row_end = end offset of its sequence.
 __global__ void k_struct_rows ( const uint32_t * __restrict__ offs, uint32_t nseq, uint64_t total, uint32_t l0,
-                                uint32_t tml, int pair_mode, uint8_t * row_ok, uint32_t * row_end )
+                                uint32_t tml, uint32_t npat, uint8_t * row_ok, uint32_t * row_end )
 {
     const uint32_t pos = blockIdx.x * blockDim.x + threadIdx.x;
     if ( pos >= total ) return;
@@ -444,7 +444,7 @@ __global__ void k_struct_rows ( const uint32_t * __restrict__ offs, uint32_t nse
     while ( offs[lo + 1] <= pos ) ++lo;
     const uint32_t start = offs[lo], end = offs[lo + 1];
     row_end[pos] = end;
-    row_ok[pos] = ( end - start ) >= tml && pos - start + 1 >= l0 && ( ! pair_mode || lo == 0 );
+    row_ok[pos] = ( end - start ) >= tml && pos - start + 1 >= l0 && ( npat == 0 || lo < npat );
 }
 
 /*

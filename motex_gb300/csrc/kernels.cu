@@ -189,11 +189,11 @@ __global__ void k_pack ( PackArgs a )
             const bool is_short = ( end - start ) < a.tml;
             code = cmap[a.raw[pos]];
             a.codes[pos] = ( uint8_t ) code;
-            // pair mode: sequence 0 is the pattern sequence (factors only),
-            // sequence 1 the text (searched only)
-            valid = ! is_short && rel >= a.vstart && ! ( a.pair_mode && s == 0 );
+            // pattern mode: sequences below npat are patterns (factors
+            // only), the rest are texts (searched only)
+            valid = ! is_short && rel >= a.vstart && s >= a.npat;
             is_end = pos == end - 1;
-            if ( ! is_short && rel + 1 >= a.l && ( ! a.pair_mode || s == 0 ) )
+            if ( ! is_short && rel + 1 >= a.l && ( a.npat == 0 || s < a.npat ) )
                 a.wpos[a.wstart[s] + ( uint32_t ) ( rel + 1 - a.l )] = ( uint32_t ) pos;
         }
         const uint32_t full = 0xffffffffu;

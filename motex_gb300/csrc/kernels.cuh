@@ -20,7 +20,7 @@ struct PackArgs
     uint32_t         l;            // factor length (box 0)
     uint32_t         tml;          // minimum sequence length (shorter ones are skipped)
     uint32_t         vstart;       // first position (relative) at which a match may end
-    int              pair_mode;
+    uint32_t         npat;         // leading pattern sequences (factors only); 0: every sequence is both
     const uint32_t * wstart;       // first factor index of each sequence
     uint8_t *        codes;
     uint32_t *       planes;
@@ -137,7 +137,7 @@ __global__ void k_seq_start ( const uint32_t * offs, uint32_t nseq, uint64_t tot
 __global__ void k_wplanes_all ( const uint8_t * codes, uint32_t total, uint32_t l, uint32_t B, int top_aligned,
                                 uint32_t * out );
 __global__ void k_struct_rows ( const uint32_t * offs, uint32_t nseq, uint64_t total, uint32_t l0, uint32_t tml,
-                                int pair_mode, uint8_t * row_ok, uint32_t * row_end );
+                                uint32_t npat, uint8_t * row_ok, uint32_t * row_end );
 __global__ void k_struct_finalize ( StructFinalizeArgs a );
 
 // DP launchers (dp.cu): return false if no kernel matches the shape.

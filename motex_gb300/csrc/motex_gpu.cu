@@ -110,7 +110,7 @@ struct Job
     uint64_t total = 0;
     uint32_t tml = 0;
     uint32_t nwords = 0;
-    bool pair_mode = false;
+    uint32_t npat = 0;                         // leading pattern sequences (0: all-pairs)
     uint64_t ref_cells = 0;
     uint32_t G = 1;                            // gap choices (1 for single motifs)
     std::vector<char> raw_host;                // structured runs: input copy for key dedup
@@ -635,7 +635,7 @@ int stage_pack ( Job * j, bool * need_sync )
     pa.l = P.l;
     pa.tml = j->tml;
     pa.vstart = ed ? 0 : P.l - 1;
-    pa.pair_mode = j->pair_mode;
+    pa.npat = j->npat;
     pa.wstart = dptr<uint32_t> ( j, S_WSTART );
     pa.codes = codes;
     pa.planes = planes;
@@ -650,7 +650,7 @@ int stage_pack ( Job * j, bool * need_sync )
     j->generic = ! j->structured && P.l > 32;
     uint32_t * scalar;
     MTX_TRY ( ensure ( j, S_SCALAR, 4, &scalar ) );
-    if ( ! j->structured && ! j->pair_mode && j->nwords > 0 )
+    if ( ! j->structured && ! j->npat && j->nwords > 0 )
     {
         uint32_t * idx;
         MTX_TRY ( sort_factors ( j, j->nwords, &idx ) );
@@ -741,7 +741,7 @@ int stage_plan ( Job * j, bool sorted )
                      wpl );
         da.wplanes64 = wpl;
     }
-    const uint32_t first_blk = j->pair_mode ? ( j->offs[1] / 32 ) : 0;
+    const uint32_t first_blk = j->npat ? ( j->offs[j->npat] / 32 ) : 0;
     const uint32_t warmup = ed ? P.l + P.e - 1 : ( j->generic ? P.l - 1 : 0 );
     const uint32_t target = ( uint32_t ) j->ctx->num_sms * 24;
     uint32_t nchunks = std::max<uint32_t> ( 1, ( target + j->ntiles - 1 ) / j->ntiles );
@@ -809,11 +809,11 @@ int plan_structured ( Job * j )
     MTX_LAUNCH ( k_wplanes_all, blocks_for ( T, 256 ), 256, codes, T, P.l, ( uint32_t ) B, ed ? 0 : 1, wpl0 );
     MTX_LAUNCH ( k_wplanes_all, blocks_for ( T, 256 ), 256, codes, T, b1, ( uint32_t ) B, ed ? 0 : 1, wpl1 );
     MTX_LAUNCH ( k_struct_rows, blocks_for ( T, 256 ), 256, dptr<uint32_t> ( j, S_OFFS ), j->nseq, j->total, P.l,
-                 j->tml, ( int ) j->pair_mode, row_ok, row_end );
+                 j->tml, j->npat, row_ok, row_end );
 
     const uint32_t ctas_x = ( T + kDPThreads - 1 ) / kDPThreads;
     j->ntiles = ctas_x;
-    const uint32_t first_blk = j->pair_mode ? ( j->offs[1] / 32 ) : 0;
+    const uint32_t first_blk = j->npat ? ( j->offs[j->npat] / 32 ) : 0;
     const uint32_t warmup = ( ed ? std::max ( P.l + P.e - 1, b1 + e1 - 1 ) : 0 ) + gmax + b1;
     uint32_t nchunks = std::max<uint32_t> ( 1, ( ( uint32_t ) j->ctx->num_sms * 24 + ctas_x - 1 ) / ctas_x );
     nchunks = std::min<uint32_t> ( nchunks, std::max<uint32_t> ( 1, ( j->nblk - first_blk ) / 16 ) );
@@ -888,7 +888,7 @@ int plan_structured_n ( Job * j )
         MTX_LAUNCH ( k_wplanes_all, blocks_for ( T, 256 ), 256, codes, T, b ? j->blens[b - 1] : P.l, ( uint32_t ) B,
                      ed ? 0 : 1, wpl + ( size_t ) b * B * T );
     MTX_LAUNCH ( k_struct_rows, blocks_for ( T, 256 ), 256, dptr<uint32_t> ( j, S_OFFS ), j->nseq, j->total, P.l,
-                 j->tml, ( int ) j->pair_mode, row_ok, row_end );
+                 j->tml, j->npat, row_ok, row_end );
     MTX_LAUNCH ( k_seq_start, blocks_for ( T, 256 ), 256, dptr<uint32_t> ( j, S_OFFS ), j->nseq, j->total, seq_start );
     // cumulative end offsets of boxes 1..NG for every structure k (motex.cc:439-486 order)
     uint32_t * h_xoff = pin<uint32_t> ( j, kPinXoff );
@@ -911,7 +911,7 @@ int plan_structured_n ( Job * j )
     MTX_CUDA ( cudaMemcpyAsync ( xoff, h_xoff, ( size_t ) NS * NG * 4, cudaMemcpyHostToDevice, st ) );
     const uint32_t ctas_x = ( T + kDPThreads - 1 ) / kDPThreads;
     j->ntiles = ctas_x;
-    const uint32_t first_blk = j->pair_mode ? ( j->offs[1] / 32 ) : 0;
+    const uint32_t first_blk = j->npat ? ( j->offs[j->npat] / 32 ) : 0;
     const uint32_t warmup = ed ? P.l + P.e - 1 : 0;
     uint32_t nchunks = std::max<uint32_t> ( 1, ( ( uint32_t ) j->ctx->num_sms * 24 + ctas_x - 1 ) / ctas_x );
     nchunks = std::min<uint32_t> ( nchunks, std::max<uint32_t> ( 1, ( j->nblk - first_blk ) / 16 ) );
@@ -1011,7 +1011,7 @@ int stage_finalize ( Job * j, bool * need_sync )
         fa.nseq = j->nseq;
         fa.nmin = P.n;
         fa.nmax = P.N;
-        if ( j->pair_mode )
+        if ( j->npat )
         {
             uint32_t *uo, *vo;
             MTX_TRY ( ensure ( j, S_UOUT, n, &uo ) );
@@ -1049,7 +1049,7 @@ int stage_finalize ( Job * j, bool * need_sync )
     fa.nmin = P.n;
     fa.nmax = P.N;
     fa.uniq_pos = j->uniq;
-    if ( j->pair_mode )
+    if ( j->npat )
     {
         uint32_t *uo, *vo;
         MTX_TRY ( ensure ( j, S_UOUT, std::max<uint32_t> ( 1, U ), &uo ) );
@@ -1080,7 +1080,7 @@ int stage_finalize ( Job * j, bool * need_sync )
 
 int stage_compact ( Job * j )
 {
-    if ( ! j->pair_mode )
+    if ( ! j->npat )
     {
         if ( ! j->replaying ) j->nrec = pin<uint32_t> ( j, kPinScalar )[1];
         const uint32_t n = ( uint32_t ) ( j->structured ? j->total * j->G : j->total );
@@ -1178,8 +1178,14 @@ int execute_job ( Job * j )
     return MOTEX_OK;
 }
 
+/*
+ * npat = 0: all-pairs (every sequence gives factors and is searched).
+ * npat > 0: sequences [0, npat) give the factors and [npat, nseq) are the
+ * texts.  skip_short applies the reference's short-sequence skip
+ * (total_mot_length > n) to the searched sequences.
+ */
 int load_job ( Job * j, const motex_params * prm, const char * const * seqs, const uint32_t * lens, uint32_t nseq,
-               bool pair_mode )
+               uint32_t npat, bool skip_short )
 {
     MTX_TRY ( validate ( prm ) );
     if ( ! seqs || ! lens ) return fail ( MOTEX_EINVAL, "null sequence arrays" );
@@ -1198,7 +1204,7 @@ int load_job ( Job * j, const motex_params * prm, const char * const * seqs, con
     j->G = 1;                                      // gap structures (lexicographic, gap 0 slowest)
     for ( uint32_t g = 0; g < prm->nb_gaps; ++g ) j->G *= j->gmax[g] - j->gmin[g] + 1;
     j->nseq = nseq;
-    j->pair_mode = pair_mode;
+    j->npat = npat;
     j->offs.assign ( nseq + 1, 0 );
     uint64_t total = 0;
     for ( uint32_t i = 0; i < nseq; ++i )
@@ -1215,20 +1221,21 @@ int load_job ( Job * j, const motex_params * prm, const char * const * seqs, con
     // total_mot_length (motex.cc:312-360): l plus minimum gaps and boxes
     uint32_t tml_full = l;
     for ( uint32_t g = 0; g < prm->nb_gaps; ++g ) tml_full += j->gmin[g] + j->blens[g];
-    j->tml = pair_mode ? 0 : tml_full;
+    j->tml = skip_short ? tml_full : 0;
     // factor ends per sequence and the reference's cell count
     std::vector<uint32_t> wstart ( nseq + 1, 0 );
-    uint64_t nw = 0, searched = 0;
+    uint64_t nw = 0, searched = 0, pattern_len = 0;
     for ( uint32_t i = 0; i < nseq; ++i )
     {
         wstart[i] = ( uint32_t ) nw;
-        const bool has_words = lens[i] >= std::max ( l, j->tml ) && ( ! pair_mode || i == 0 );
+        const bool has_words = lens[i] >= std::max ( l, j->tml ) && ( npat == 0 || i < npat );
         if ( has_words ) nw += lens[i] - l + 1;
-        if ( lens[i] >= j->tml ) searched += lens[i];
+        if ( i < npat ) pattern_len += lens[i];
+        else if ( lens[i] >= j->tml ) searched += lens[i];
     }
     wstart[nseq] = ( uint32_t ) nw;
     j->nwords = ( uint32_t ) nw;
-    j->ref_cells = ( pair_mode ? ( uint64_t ) lens[0] * lens[1] : searched * searched ) * ( prm->nb_gaps + 1 );
+    j->ref_cells = ( npat ? pattern_len * searched : searched * searched ) * ( prm->nb_gaps + 1 );
     // qok[u]: the reference's double-precision quorum test (functions.cc:1105-1108)
     std::vector<uint8_t> qok ( nseq + 1 );
     for ( uint32_t u = 0; u <= nseq; ++u )
@@ -1247,7 +1254,7 @@ int load_job ( Job * j, const motex_params * prm, const char * const * seqs, con
         memcpy ( stage + at, seqs[i], lens[i] );
         at += lens[i];
     }
-    if ( prm->nb_gaps && ! pair_mode ) j->raw_host.assign ( stage, stage + total );
+    if ( prm->nb_gaps && ! npat ) j->raw_host.assign ( stage, stage + total );
     else j->raw_host.clear ();
     memcpy ( stage + raw_b, j->offs.data (), ( size_t ) ( nseq + 1 ) * 4 );
     memcpy ( stage + raw_b + offs_b, wstart.data (), ( size_t ) ( nseq + 1 ) * 4 );
@@ -1500,14 +1507,14 @@ int motex_gpu_load ( motex_ctx * c, const motex_params * prm, const char * const
 {
     if ( ! c ) return fail ( MOTEX_EINVAL, "null context" );
     MTX_CUDA ( cudaSetDevice ( c->device ) );
-    return load_job ( &c->main, prm, seqs, lens, nseq, false );
+    return load_job ( &c->main, prm, seqs, lens, nseq, 0, true );
 }
 
 int motex_gpu_execute ( motex_ctx * c )
 {
     if ( ! c ) return fail ( MOTEX_EINVAL, "null context" );
     Job * j = &c->main;
-    if ( ! j->loaded || j->pair_mode ) return fail ( MOTEX_EINVAL, "no sequences loaded" );
+    if ( ! j->loaded || j->npat ) return fail ( MOTEX_EINVAL, "no sequences loaded" );
     MTX_CUDA ( cudaSetDevice ( c->device ) );
     MTX_TRY ( execute_job ( j ) );
     j->executed = true;
@@ -1545,7 +1552,7 @@ int motex_gpu_run_batch ( motex_ctx * c, const motex_job * jobs, uint32_t njobs,
         js[i] = c->pool[i].get ();
         js[i]->replaying = false;
         js[i]->batched = true;
-        MTX_TRY ( load_job ( js[i], jobs[i].prm, jobs[i].seqs, jobs[i].lens, jobs[i].nseq, false ) );
+        MTX_TRY ( load_job ( js[i], jobs[i].prm, jobs[i].seqs, jobs[i].lens, jobs[i].nseq, 0, true ) );
     }
     for ( Job * j : js ) MTX_TRY ( stage_presence ( j ) );
     MTX_TRY ( sync ( c ) );
@@ -1598,7 +1605,7 @@ int motex_gpu_extract_pair ( motex_ctx * c, const motex_params * prm, const char
     const char * seqs[2] = { p, t };
     const uint32_t lens[2] = { m, n };
     Job * j = &c->main;
-    MTX_TRY ( load_job ( j, prm, seqs, lens, 2, true ) );
+    MTX_TRY ( load_job ( j, prm, seqs, lens, 2, 1, false ) );
     j->replaying = false;
     MTX_TRY ( run_job ( j ) );
     MTX_TRY ( read_times ( j ) );
@@ -1629,6 +1636,60 @@ int motex_gpu_extract_pair ( motex_ctx * c, const motex_params * prm, const char
             u[prm->l - 1 + w] += hu[w];
             v[prm->l - 1 + w] += hv[w];
         }
+    j->loaded = false;
+    return MOTEX_OK;
+}
+
+int motex_gpu_search ( motex_ctx * c, const motex_params * prm, const char * const * words, const uint32_t * wlens,
+                       uint32_t nwords, const char * const * seqs, const uint32_t * lens, uint32_t nseq,
+                       uint32_t * u, uint32_t * v )
+{
+    if ( ! c || ! prm ) return fail ( MOTEX_EINVAL, "null argument" );
+    if ( nwords && ( ! words || ! wlens || ! u || ! v ) ) return fail ( MOTEX_EINVAL, "null word arrays" );
+    if ( nseq && ( ! seqs || ! lens ) ) return fail ( MOTEX_EINVAL, "null sequence arrays" );
+    if ( prm->nb_gaps ) return fail ( MOTEX_EUNSUPPORTED, "the word search takes plain motifs only" );
+    MTX_TRY ( validate ( prm ) );
+    MTX_CUDA ( cudaSetDevice ( c->device ) );
+    const uint32_t l = prm->l;
+    for ( uint32_t i = 0; i < nwords; ++i ) u[i] = v[i] = 0;
+    // patterns: the last l symbols of every word long enough, then the sequences
+    std::vector<const char *> all;
+    std::vector<uint32_t> alens, which;
+    for ( uint32_t i = 0; i < nwords; ++i )
+    {
+        if ( wlens[i] < l ) continue;
+        if ( ! words[i] ) return fail ( MOTEX_EINVAL, "null word %u", i );
+        all.push_back ( words[i] + wlens[i] - l );
+        alens.push_back ( l );
+        which.push_back ( i );
+    }
+    const uint32_t npat = ( uint32_t ) which.size ();
+    bool searched = false;
+    for ( uint32_t s = 0; s < nseq; ++s )
+    {
+        all.push_back ( seqs[s] );
+        alens.push_back ( lens[s] );
+        searched |= lens[s] >= l;
+    }
+    if ( npat == 0 || ! searched ) return MOTEX_OK;
+    Job * j = &c->main;
+    MTX_TRY ( load_job ( j, prm, all.data (), alens.data (), ( uint32_t ) all.size (), npat, true ) );
+    j->replaying = false;
+    MTX_TRY ( run_job ( j ) );
+    MTX_TRY ( read_times ( j ) );
+    if ( j->U != npat ) return fail ( MOTEX_ECUDA, "word search planned %u factors for %u words", j->U, npat );
+    const size_t bytes = ( size_t ) npat * 4;
+    MTX_TRY ( ensure_pinned ( j, kPinStage + 2 * bytes ) );
+    uint32_t * hu = pin<uint32_t> ( j, kPinStage );
+    uint32_t * hv = hu + npat;
+    MTX_CUDA ( cudaMemcpyAsync ( hu, dptr<uint32_t> ( j, S_UOUT ), bytes, cudaMemcpyDeviceToHost, c->st ) );
+    MTX_CUDA ( cudaMemcpyAsync ( hv, dptr<uint32_t> ( j, S_VOUT ), bytes, cudaMemcpyDeviceToHost, c->st ) );
+    MTX_TRY ( sync ( c ) );
+    for ( uint32_t w = 0; w < npat; ++w )
+    {
+        u[which[w]] = hu[w];
+        v[which[w]] = hv[w];
+    }
     j->loaded = false;
     return MOTEX_OK;
 }

@@ -16,11 +16,15 @@
  *   SMILE-like file (-S)    functions.cc:1262-1461 (header, plain motifs)
  *                           and 1463-1591 (structured motifs)
  *   option combinations     motex.cc:147-201
+ *   background (-b -u -U)   functions.cc:1613-2238 (-o and -u files),
+ *                           2241-2748 (the -S/-U pair)
+ *   word search (-I)        motex.cc:883-1137, functions.cc:2750-2829;
+ *                           the counting runs on the GPU (motex_gpu_search)
+ *   binomial tail           binomial.cc:78-103 (the long double flavour:
+ *                           the reference built without MPFR)
  * Differences: -L <int> is accepted as a real switch (the reference compiles
- * it out and getopt reports it as invalid; the output is the same), -t is
- * accepted and ignored, and the background / unmatched-motif modes
- * (-b -u -U -I) are rejected after the reference's own checks of their
- * combinations.
+ * it out and getopt reports it as invalid; the output is the same) and -t is
+ * accepted and ignored.
  *
  * Set MOTEX_METRICS=<file> to append a JSON line with the run's cell counts,
  * device time and GCUPS.
@@ -36,7 +40,9 @@
 #include <sys/time.h>
 #include <time.h>
 
+#include <algorithm>
 #include <string>
+#include <unordered_map>
 #include <vector>
 
 static const char * const ALPHA_DNA = "ACGTN";
@@ -202,9 +208,8 @@ static void write_header ( FILE * out, const Switches & sw, const motex_params &
  * string ('0' + rank in the alphabet string, '-' for a separator), u, a tab
  * and v.  The motif set and order are those of the main output.
  */
-static void write_smile ( FILE * out, const Switches & sw, const motex_params & P, unsigned num_seqs,
-                          unsigned total_length, const char * alphabet, const std::vector<std::string> & words,
-                          const motex_result & res, double secs )
+static void write_smile_header ( FILE * out, const Switches & sw, const motex_params & P, unsigned num_seqs,
+                                 unsigned total_length, const char * alphabet )
 {
     char buf[128];
     const int quorum = ( int ) ceil ( ( double ) ( ( double ) sw.q * num_seqs ) / ( double ) 100 );
@@ -243,22 +248,273 @@ static void write_smile ( FILE * out, const Switches & sw, const motex_params & 
         fprintf ( out, "\n%s\n", blank.c_str () );
     }
     fprintf ( out, "%s\n", std::string ( 79, '=' ).c_str () );
+}
 
+static void write_smile_line ( FILE * out, const motex_params & P, const char * alphabet, const std::string & w,
+                               uint32_t u, uint32_t v )
+{
     const size_t na = strlen ( alphabet );
-    std::string id;
+    std::string id ( w.size (), '-' );
+    for ( size_t i = 0; i < w.size (); ++i )
+    {
+        const char * at = w[i] ? ( const char * ) memchr ( alphabet, w[i], na ) : nullptr;
+        id[i] = at ? ( char ) ( '0' + ( at - alphabet ) ) : ( P.nb_gaps ? '-' : ( char ) ( '0' + na ) );
+    }
+    fprintf ( out, "%s %s %d\t%d\n", w.c_str (), id.c_str (), u, v );
+}
+
+/*
+ * P(X < x) for X ~ Bin(N, p), 0 when p >= 1 (binomial.cc:78-103, the long
+ * double flavour).  fact[i] = i!.  The terms are formed and summed in the
+ * reference's order so that the rounding, and so the printed tail
+ * 1 - P(X < x), is the same on a host with the same long double format.
+ */
+static std::vector<long double> factorials ( unsigned n )
+{
+    std::vector<long double> f ( ( size_t ) n + 1 );
+    f[0] = 1;
+    for ( unsigned i = 1; i <= n; ++i ) f[i] = f[i - 1] * i;
+    return f;
+}
+
+static long double binomial_below ( int x, int N, long double p, const std::vector<long double> & fact )
+{
+    long double sum = 0.;
+    if ( p >= 1.0 ) return 0.;
+    for ( int i = 0; i < x; ++i )
+    {
+        const long double term = ( fact[N] / fact[i] ) / fact[N - i] * powl ( p, ( long double ) i ) *
+                                 powl ( 1. - p, ( long double ) ( N - i ) );
+        sum += term;
+        if ( x > N ) break;
+    }
+    return sum;
+}
+
+/*
+ * A MoTeX output file read as a background (functions.cc:1683-1757): header
+ * line 6 ("# For N input sequences") gives N, line 8 ("#     q = Q") gives Q;
+ * after the header's blank line, one motif per line up to the next blank
+ * line: its key (the first klen symbols), u, n, r and v.  A repeated key
+ * keeps its last row.
+ */
+struct Background
+{
+    struct Row
+    {
+        unsigned u = 0, n = 0, v = 0;
+        double r = 0;
+    };
+    int size = 0, quorum = 0;
+    std::unordered_map<std::string, int> index;       // key -> row; -1 once printed
+    std::vector<Row> rows;
+};
+
+static bool read_background ( const char * path, size_t klen, Background & bg )
+{
+    FILE * in = fopen ( path, "r" );
+    if ( ! in ) return false;
+    char line[512];
+    std::string size_field, quorum_field;
+    for ( unsigned ln = 1; fgets ( line, sizeof line, in ) && line[0] != '\n'; ++ln )
+    {
+        if ( ln != 6 && ln != 8 ) continue;
+        char * save = nullptr;
+        char * f = strtok_r ( line, " ", &save );
+        for ( int k = 0; k < 2 && f; ++k ) f = strtok_r ( nullptr, " ", &save );
+        if ( ln == 8 && f ) f = strtok_r ( nullptr, "\n", &save );
+        ( ln == 6 ? size_field : quorum_field ) = f ? f : "";
+    }
+    bg.size = atoi ( size_field.c_str () );
+    bg.quorum = atoi ( quorum_field.c_str () );
+    while ( fgets ( line, sizeof line, in ) && line[0] != '\n' )
+    {
+        char * save = nullptr;
+        char * key = strtok_r ( line, " ", &save );
+        if ( ! key ) continue;
+        const char * f[4] = {};
+        for ( int k = 0; k < 4; ++k ) f[k] = strtok_r ( nullptr, " ", &save );
+        Background::Row row;
+        row.u = ( unsigned ) atoi ( f[0] ? f[0] : "0" );
+        row.n = ( unsigned ) atoi ( f[1] ? f[1] : "0" );
+        row.r = atof ( f[2] ? f[2] : "0" );
+        row.v = ( unsigned ) atoi ( f[3] ? f[3] : "0" );
+        bg.index[std::string ( key, strnlen ( key, klen ) )] = ( int ) bg.rows.size ();
+        bg.rows.push_back ( row );
+    }
+    fclose ( in );
+    return true;
+}
+
+/*
+ * -I (motex.cc:883-1137): the motif file is read from after its first blank
+ * line up to the next one, one "motif u n r v" per line; the GPU counts
+ * every motif's last factor in every sequence at least l long, and
+ * write_motifs_fore (functions.cc:2750-2829) prints the passing ones with
+ * the file's u n r v, the new u/N and v, and 1 - P(X < u_file) for
+ * X ~ Bin(n_file, u/N).
+ */
+static int run_foreground ( const Switches & sw, const motex_params & P, const std::vector<std::string> & seqs )
+{
+    FILE * in = fopen ( sw.un_in_filename, "r" );
+    if ( ! in ) { fprintf ( stderr, " Error: Cannot open file %s!\n", sw.un_in_filename ); return 1; }
+    char line[512];
+    while ( fgets ( line, sizeof line, in ) && line[0] != '\n' );
+    std::vector<std::string> motifs;
+    std::vector<Background::Row> given;
+    while ( fgets ( line, sizeof line, in ) && line[0] != '\n' )
+    {
+        char * save = nullptr;
+        char * word = strtok_r ( line, " ", &save );
+        const char * f[4] = {};
+        for ( int k = 0; k < 4 && word; ++k ) f[k] = strtok_r ( nullptr, " ", &save );
+        if ( ! word || ! f[3] )
+        {
+            fprintf ( stderr, " Error: file %s is not in the correct format!\n", sw.un_in_filename );
+            fclose ( in );
+            return 1;
+        }
+        motifs.push_back ( word );
+        Background::Row row;
+        row.u = ( unsigned ) atoi ( f[0] );
+        row.n = ( unsigned ) atoi ( f[1] );
+        row.r = atof ( f[2] );
+        row.v = ( unsigned ) atoi ( f[3] );
+        given.push_back ( row );
+    }
+    if ( fclose ( in ) ) { fprintf ( stderr, " Error: file close error!\n" ); return 1; }
+
+    const unsigned num_seqs = ( unsigned ) seqs.size (), nm = ( unsigned ) motifs.size ();
+    std::vector<const char *> wptr ( nm ), sptr ( num_seqs );
+    std::vector<uint32_t> wlen ( nm ), slen ( num_seqs ), u ( nm ), v ( nm );
+    for ( unsigned i = 0; i < nm; ++i ) { wptr[i] = motifs[i].data (); wlen[i] = ( uint32_t ) motifs[i].size (); }
+    for ( unsigned s = 0; s < num_seqs; ++s ) { sptr[s] = seqs[s].data (); slen[s] = ( uint32_t ) seqs[s].size (); }
+    motex_ctx * ctx = nullptr;
+    int rc = motex_ctx_create ( &ctx, 0 );
+    if ( rc != MOTEX_OK ) { fprintf ( stderr, " Error: %s: %s\n", motex_gpu_strerror ( rc ), motex_gpu_last_error () ); return 1; }
+    double start = gettime ();
+    rc = motex_gpu_search ( ctx, &P, wptr.data (), wlen.data (), nm, sptr.data (), slen.data (), num_seqs, u.data (), v.data () );
+    double end = gettime ();
+    motex_ctx_destroy ( ctx );
+    if ( rc != MOTEX_OK )
+    {
+        fprintf ( stderr, " Error: word search failed: %s: %s\n", motex_gpu_strerror ( rc ), motex_gpu_last_error () );
+        return 1;
+    }
+
+    FILE * out = fopen ( sw.output_filename, "w" );
+    if ( ! out ) { fprintf ( stderr, " Error: cannot open file!\n" ); return 0; }
+    write_header ( out, sw, P, num_seqs, end - start );
+    unsigned top = num_seqs;
+    for ( const Background::Row & g : given ) top = std::max ( top, g.n );
+    const std::vector<long double> fact = factorials ( top );
+    unsigned valid = 0;
+    for ( unsigned i = 0; i < nm; ++i )
+    {
+        if ( motifs[i].empty () ) continue;
+        const double ratio = ( double ) u[i] / num_seqs;
+        const double pct = ratio * 100;
+        if ( ! ( pct >= sw.q && v[i] >= sw.n && pct <= sw.Q && v[i] <= sw.N ) ) continue;
+        const long double below = binomial_below ( ( int ) given[i].u, ( int ) given[i].n, ( long double ) u[i] / num_seqs, fact );
+        fprintf ( out, "%s %d %d %lf %d %lf %d %Le\n", motifs[i].c_str (), given[i].u, given[i].n, given[i].r, given[i].v,
+                  ratio, v[i], 1. - below );
+        valid++;
+    }
+    fprintf ( out, "\n#A total of %d valid motifs were extracted.\n\n", valid );
+    if ( fclose ( out ) ) fprintf ( stderr, " Error: file close error!\n" );
+    return 0;
+}
+
+/*
+ * -b (functions.cc:1613-2238): each printed motif either matches a row of
+ * the background not yet matched -- printed with that row's r and v and
+ * 1 - P(X < u), X ~ Bin(N, row u) -- or is unmatched: printed with "0 0"
+ * and 1 - P(X < u), X ~ Bin(N, Q_bg / N_bg), and also written to the -u
+ * file.  With -U the same split goes to the -S/-U SMILE-like pair
+ * (functions.cc:2241-2748).  Returns false on the reference's assertion
+ * of a background without a sequence count or quorum.
+ */
+static bool write_background ( const Switches & sw, const motex_params & P, unsigned num_seqs, unsigned total_length,
+                               const char * alphabet, const std::vector<std::string> & words, const motex_result & res,
+                               double secs )
+{
+    size_t klen = sw.l;
+    for ( unsigned g = 0; g < P.nb_gaps; ++g ) klen += P.blens[g] + 1;
+    FILE * out = fopen ( sw.output_filename, "w" );
+    if ( ! out ) { fprintf ( stderr, " Error: cannot open file!\n" ); return true; }
+    write_header ( out, sw, P, num_seqs, secs );
+    FILE * un = fopen ( sw.un_out_filename, "w" );
+    if ( ! un ) { fprintf ( stderr, " Error: cannot open file!\n" ); fclose ( out ); return true; }
+    write_header ( un, sw, P, num_seqs, secs );
+    Background bg;
+    if ( ! read_background ( sw.background_in_filename, klen, bg ) )
+    {
+        fprintf ( stderr, " Error: cannot open file!\n" );
+        fclose ( out );
+        fclose ( un );
+        return true;
+    }
+    if ( ! ( bg.size > 0 && bg.quorum > 0 ) )
+    {
+        fprintf ( stderr, " Error: background file %s gives no sequence count or no quorum!\n", sw.background_in_filename );
+        fclose ( out );
+        fclose ( un );
+        return false;
+    }
+    const std::vector<long double> fact = factorials ( num_seqs );
+    const long double p_bg = ( long double ) bg.quorum / bg.size;
+    std::vector<char> matched ( res.count, 0 );
+    unsigned pvalid = 0, uvalid = 0;
     for ( uint32_t r = 0; r < res.count; ++r )
     {
-        const std::string & w = words[r];
-        id.resize ( w.size () );
-        for ( size_t i = 0; i < w.size (); ++i )
+        const motex_motif & m = res.motifs[r];
+        const double ratio = ( double ) m.u / num_seqs;
+        auto it = bg.index.find ( words[r] );
+        if ( it != bg.index.end () && it->second >= 0 )
         {
-            const char * at = w[i] ? ( const char * ) memchr ( alphabet, w[i], na ) : nullptr;
-            id[i] = at ? ( char ) ( '0' + ( at - alphabet ) ) : ( P.nb_gaps ? '-' : ( char ) ( '0' + na ) );
+            const Background::Row & row = bg.rows[it->second];
+            const long double below = binomial_below ( ( int ) m.u, ( int ) num_seqs, ( long double ) row.u, fact );
+            fprintf ( out, "%s %d %d %lf %d %lf %d %Le\n", words[r].c_str (), m.u, num_seqs, ratio, m.v, row.r, row.v,
+                      1. - below );
+            matched[r] = 1;
+            pvalid++;
         }
-        fprintf ( out, "%s %s %d\t%d\n", w.c_str (), id.c_str (), res.motifs[r].u, res.motifs[r].v );
+        else
+        {
+            const long double below = binomial_below ( ( int ) m.u, ( int ) num_seqs, p_bg, fact );
+            fprintf ( out, "%s %d %d %lf %d %d %d %Le\n", words[r].c_str (), m.u, num_seqs, ratio, m.v, 0, 0, 1. - below );
+            fprintf ( un, "%s %d %d %lf %d\n", words[r].c_str (), m.u, num_seqs, ratio, m.v );
+            uvalid++;
+        }
+        bg.index[words[r]] = -1;
     }
-    fprintf ( out, "Nb models: %d\n", res.count );
-    fprintf ( out, "User time: %lf sec.\n", secs );
+    fprintf ( out, "\n#A total of %d background motifs were read.\n", ( int ) bg.rows.size () );
+    fprintf ( out, "#A total of %d valid motifs were extracted:\n", pvalid + uvalid );
+    fprintf ( out, "#  %d of them were matched with background motifs\n", pvalid );
+    fprintf ( out, "#  %d of them were not matched with any background motif.\n\n", uvalid );
+    fprintf ( un, "\n#A total of %d background motifs were read.\n", ( int ) bg.rows.size () );
+    fprintf ( un, "#A total of %d valid motifs were extracted:\n", pvalid + uvalid );
+    fprintf ( un, "#  %d of them were not matched with any background motif.\n\n", uvalid );
+    if ( fclose ( out ) || fclose ( un ) ) fprintf ( stderr, " Error: file close error!\n" );
+    if ( ! sw.un_smile_out_filename ) return true;
+
+    FILE * usm = fopen ( sw.un_smile_out_filename, "w" );
+    if ( ! usm ) { fprintf ( stderr, " Error: cannot open file %s!\n", sw.un_smile_out_filename ); return true; }
+    write_smile_header ( usm, sw, P, num_seqs, total_length, alphabet );
+    FILE * sm = fopen ( sw.smile_out_filename, "w" );
+    if ( ! sm ) { fprintf ( stderr, " Error: cannot open file %s!\n", sw.smile_out_filename ); fclose ( usm ); return true; }
+    write_smile_header ( sm, sw, P, num_seqs, total_length, alphabet );
+    for ( uint32_t r = 0; r < res.count; ++r )
+    {
+        if ( ! matched[r] ) write_smile_line ( usm, P, alphabet, words[r], res.motifs[r].u, res.motifs[r].v );
+        write_smile_line ( sm, P, alphabet, words[r], res.motifs[r].u, res.motifs[r].v );
+    }
+    fprintf ( sm, "Nb models: %d\n", pvalid + uvalid );
+    fprintf ( sm, "User time: %lf sec.\n", secs );
+    fprintf ( usm, "Nb models: %d\n", uvalid );
+    fprintf ( usm, "User time: %lf sec.\n", secs );
+    if ( fclose ( usm ) || fclose ( sm ) ) fprintf ( stderr, " Error: file close error!\n" );
+    return true;
 }
 
 int main ( int argc, char ** argv )
@@ -302,11 +558,6 @@ int main ( int argc, char ** argv )
     if ( sw.boxes_in_filename && sw.un_in_filename )
     {
         fprintf ( stderr, " Error: `-I' option cannot be used with `-s' option!\n" );
-        return 1;
-    }
-    if ( sw.background_in_filename || sw.un_in_filename )
-    {
-        fprintf ( stderr, " Error: the background and unmatched-motif modes (-b -u -U -I) are not part of motexGPU!\n" );
         return 1;
     }
 
@@ -362,6 +613,8 @@ int main ( int argc, char ** argv )
         P.gap_min = gmin.data (); P.gap_max = gmax.data (); P.blens = blens.data (); P.berrs = berrs.data ();
     }
 
+    if ( sw.un_in_filename ) return run_foreground ( sw, P, seqs );
+
     std::vector<const char *> ptrs ( seqs.size () );
     std::vector<uint32_t> lens ( seqs.size () );
     for ( size_t s = 0; s < seqs.size (); ++s ) { ptrs[s] = seqs[s].data (); lens[s] = ( uint32_t ) seqs[s].size (); }
@@ -413,34 +666,51 @@ int main ( int argc, char ** argv )
         }
     }
 
+    unsigned total_length = 0;
+    for ( const std::string & q : seqs ) total_length += ( unsigned ) q.size ();
+
     /* a file that cannot be opened is reported and skipped; the exit status
        stays 0, as the reference ignores its writers' status (motex.cc:836-866) */
-    FILE * out = fopen ( sw.output_filename, "w" );
-    if ( ! out ) fprintf ( stderr, " Error: cannot open file!\n" );
+    if ( sw.background_in_filename )
+    {
+        if ( ! write_background ( sw, P, num_seqs, total_length, alphabet, words, res, end - start ) )
+        {
+            motex_result_free ( &res );
+            motex_ctx_destroy ( ctx );
+            return 1;
+        }
+    }
     else
     {
-        write_header ( out, sw, P, num_seqs, end - start );
-        for ( uint32_t r = 0; r < res.count; ++r )
+        FILE * out = fopen ( sw.output_filename, "w" );
+        if ( ! out ) fprintf ( stderr, " Error: cannot open file!\n" );
+        else
         {
-            const motex_motif & m = res.motifs[r];
-            fprintf ( out, "%s %d %d %lf %d\n", words[r].c_str (), m.u, num_seqs, ( double ) m.u / num_seqs, m.v );
+            write_header ( out, sw, P, num_seqs, end - start );
+            for ( uint32_t r = 0; r < res.count; ++r )
+            {
+                const motex_motif & m = res.motifs[r];
+                fprintf ( out, "%s %d %d %lf %d\n", words[r].c_str (), m.u, num_seqs, ( double ) m.u / num_seqs, m.v );
+            }
+            if ( P.nb_gaps )
+                fprintf ( out, "\n#A total of %d valid structured motifs were extracted.\n\n", res.count );
+            else
+                fprintf ( out, "\n#A total of %d valid motifs were extracted.\n\n", res.count );
+            if ( fclose ( out ) ) fprintf ( stderr, " Error: file close error!\n" );
         }
-        if ( P.nb_gaps )
-            fprintf ( out, "\n#A total of %d valid structured motifs were extracted.\n\n", res.count );
-        else
-            fprintf ( out, "\n#A total of %d valid motifs were extracted.\n\n", res.count );
-        if ( fclose ( out ) ) fprintf ( stderr, " Error: file close error!\n" );
-    }
-    if ( sw.smile_out_filename )
-    {
-        FILE * so = fopen ( sw.smile_out_filename, "w" );
-        if ( ! so ) fprintf ( stderr, " Error: cannot open file!\n" );
-        else
+        if ( sw.smile_out_filename )
         {
-            unsigned total_length = 0;
-            for ( const std::string & q : seqs ) total_length += ( unsigned ) q.size ();
-            write_smile ( so, sw, P, num_seqs, total_length, alphabet, words, res, end - start );
-            if ( fclose ( so ) ) fprintf ( stderr, " Error: file close error!\n" );
+            FILE * so = fopen ( sw.smile_out_filename, "w" );
+            if ( ! so ) fprintf ( stderr, " Error: cannot open file!\n" );
+            else
+            {
+                write_smile_header ( so, sw, P, num_seqs, total_length, alphabet );
+                for ( uint32_t r = 0; r < res.count; ++r )
+                    write_smile_line ( so, P, alphabet, words[r], res.motifs[r].u, res.motifs[r].v );
+                fprintf ( so, "Nb models: %d\n", res.count );
+                fprintf ( so, "User time: %lf sec.\n", end - start );
+                if ( fclose ( so ) ) fprintf ( stderr, " Error: file close error!\n" );
+            }
         }
     }
 

@@ -23,7 +23,7 @@ EXPORTS = [
     "motex_ctx_create", "motex_ctx_destroy", "motex_gpu_run", "motex_result_free",
     "motex_gpu_load", "motex_gpu_execute", "motex_gpu_fetch", "motex_gpu_extract_pair",
     "motex_gpu_strerror", "motex_gpu_last_error", "motex_ctx_launches", "motex_probe_int_peak",
-    "motex_gpu_extract_pair_static", "motex_gpu_run_batch",
+    "motex_gpu_extract_pair_static", "motex_gpu_run_batch", "motex_gpu_search",
     "motex_srv_create", "motex_srv_submit", "motex_srv_wait", "motex_srv_stats_get", "motex_srv_destroy",
 ]
 
@@ -90,6 +90,8 @@ def load_library(path: str = LIB_PATH):
         "motex_gpu_fetch": (C.c_int, [C.c_void_p, P(Result)]),
         "motex_gpu_extract_pair": (C.c_int, [C.c_void_p, P(Params), C.c_char_p, C.c_uint32, C.c_char_p,
                                              C.c_uint32, P(C.c_uint32), P(C.c_uint32)]),
+        "motex_gpu_search": (C.c_int, [C.c_void_p, P(Params), P(C.c_char_p), P(C.c_uint32), C.c_uint32,
+                                       P(C.c_char_p), P(C.c_uint32), C.c_uint32, P(C.c_uint32), P(C.c_uint32)]),
         "motex_gpu_strerror": (C.c_char_p, [C.c_int]),
         "motex_gpu_last_error": (C.c_char_p, []),
         "motex_ctx_launches": (C.c_uint64, [C.c_void_p]),
@@ -239,6 +241,15 @@ class Context:
         V = (C.c_uint32 * (m * nb_structs))(*(v or [0] * (m * nb_structs)))
         _check(self.lib.motex_gpu_extract_pair(self.h, C.byref(params), p.encode(), m, t.encode(), len(t), U, V))
         return list(U), list(V)
+
+    def search(self, words, seqs, params: Params):
+        """u, v of each word's last l symbols over the sequences (motex_gpu_search)."""
+        wb, warr, wlens = self._seq_arrays(words)
+        sb, sarr, slens = self._seq_arrays(seqs)
+        U = (C.c_uint32 * max(1, len(wb)))()
+        V = (C.c_uint32 * max(1, len(wb)))()
+        _check(self.lib.motex_gpu_search(self.h, C.byref(params), warr, wlens, len(wb), sarr, slens, len(sb), U, V))
+        return list(U)[:len(wb)], list(V)[:len(wb)]
 
 
 class Server:

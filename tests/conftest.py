@@ -1,3 +1,4 @@
+import json
 import os
 import subprocess
 import sys
@@ -41,10 +42,25 @@ def gpu_ctx(native_built):
     ctx.close()
 
 
-def golden_cases():
+def _case_dirs():
     if not os.path.isdir(GOLDEN):
         return []
     return sorted(d for d in os.listdir(GOLDEN) if os.path.isdir(os.path.join(GOLDEN, d)))
+
+
+def _has_outputs(name):
+    with open(os.path.join(GOLDEN, name, "case.json")) as f:
+        return "outputs" in json.load(f)
+
+
+def golden_cases():
+    """Cases with one main output (plus an optional SMILE-like file)."""
+    return [d for d in _case_dirs() if not _has_outputs(d)]
+
+
+def mode_cases():
+    """Background (-b) and word-search (-I) cases: several output files."""
+    return [d for d in _case_dirs() if _has_outputs(d)]
 
 
 def strip_volatile(text: str) -> str:

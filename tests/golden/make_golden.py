@@ -8,7 +8,13 @@ oracle (oracle/_build/motex_port) is run on every case as well and must give
 the identical file; a mismatch aborts the script.
 
 Cases listed in SMILE_CASES also run with ``-S out.smile`` and store the
-SMILE-like file as expected.smile.
+SMILE-like file as expected.smile.  The background cases (-b, with -u and
+optionally -S/-U) and the word-search cases (-I) of mode_cases() carry extra
+inputs -- a background file made by the reference from other seeded
+sequences, or the unmatched-motif file of such a run -- kept byte for byte
+(the reference finds N and Q in a background header by line number), and
+list their output files in case.json ("outputs"; the expected copy of X is
+expected.X, with out.motex -> expected.motex and out.smile -> expected.smile).
 
 The two non-deterministic header lines (``# Rundate:`` and ``# Run on ...``)
 and the SMILE file's ``User time:`` line are removed from stored outputs.  Cases run with relative paths (in.fa,
@@ -48,6 +54,24 @@ SMILE_CASES = {"c1_dna_hd_64x500", "prot_hd_20seq", "prot_ed_20seq", "usr_hd", "
 def strip_volatile(text: str) -> str:
     return "".join(l for l in text.splitlines(True)
                    if not l.startswith(("# Rundate:", "# Run on ", "User time:")))
+
+
+def expected_name(output):
+    return "expected." + (output[4:] if output.startswith("out.") else output)
+
+
+def run_outputs(binary, args, cwd, outputs):
+    """Returns (rc, {output name: stripped text or None})."""
+    p = subprocess.run([binary] + args, cwd=cwd, capture_output=True, text=True)
+    got = {}
+    for name in outputs:
+        path = os.path.join(cwd, name)
+        got[name] = None
+        if os.path.exists(path):
+            with open(path) as f:
+                got[name] = strip_volatile(f.read())
+            os.remove(path)
+    return p.returncode, got
 
 
 def run_cli(binary, args, cwd):
@@ -218,6 +242,93 @@ def cases():
     return out
 
 
+# ------------------------------------------------------- background and -I
+
+def _mixed_background(rng_seed, fg_seqs, alphabet, n_new, length_range, keep):
+    """Background sequences: `keep` of the foreground sequences (so some
+    motifs match) and n_new fresh random ones."""
+    rng = np.random.default_rng(rng_seed)
+    new = [W._rand_seq(rng, alphabet, int(rng.integers(*length_range))) for _ in range(n_new)]
+    return list(fg_seqs[:keep]) + new
+
+
+def mode_cases():
+    """(name, fg workload, bg sequences, background quorum, extra switches
+    for the foreground run, kind) with kind "b" (background run) or "I"
+    (search the unmatched motifs of that background run in the background
+    sequences, every motif printed: -q 0 -n 0)."""
+    out = []
+    # sequence lengths stay clear of 440-500: in the reference's -I mode a
+    # sequence copy of that size takes the memory of the closed FASTA stream
+    # it still reads the motif file's header through (motex.cc:902)
+    w = W.dna_ed(seed=2, scale=0.01, d=0)
+    w.k, w.e, w.q = 10, 1, 25
+    bgd = _mixed_background(51, w.seqs, W.DNA, 10, (600, 1000), 6)
+    out.append(("bg_dna_hd_smile", w, bgd, 10, ["-S", "out.smile", "-U", "un.smile"], "b"))
+    out.append(("fore_dna_hd", w, bgd, 10, [], "I"))
+    w = W.prot_uneven(seed=3, scale=0.01, d=1)
+    w.k, w.e, w.q = 6, 1, 10
+    w.seqs = [q for q in w.seqs if not 440 <= len(q) <= 500]
+    bgp = _mixed_background(52, w.seqs, W.AMINO20, 14, (80, 440), 10)
+    out.append(("bg_prot_ed", w, bgp, 10, [], "b"))
+    out.append(("fore_prot_ed", w, bgp, 10, [], "I"))
+    ws = planted_structured(11, 16, 150, 0)
+    out.append(("bg_struct_hd_smile", ws, _mixed_background(53, ws.seqs, W.DNA, 12, (100, 200), 9), 20,
+                ["-S", "out.smile", "-U", "un.smile"], "b"))
+    ws2 = planted_structured2(22, 14, 160, 1)
+    out.append(("bg_struct2_ed", ws2, _mixed_background(54, ws2.seqs, W.DNA, 10, (120, 200), 8), 15, [], "b"))
+    return out
+
+
+def build_mode_case(name, w, bg_seqs, bg_q, extra, kind):
+    d = os.path.join(CASES_DIR, name)
+    if os.path.isdir(d):
+        shutil.rmtree(d)
+    os.makedirs(d)
+    boxes = "in.boxes" if w.boxes else None
+    fg_args = w.cli("in.fa", "out.motex", boxes)
+    bg_args = list(fg_args)
+    bg_args[bg_args.index("-i") + 1] = "bg.fa"
+    bg_args[bg_args.index("-o") + 1] = "bg.motex"
+    bg_args[bg_args.index("-q") + 1] = str(bg_q)
+    ref_bin = os.path.join(REF, "motexCPU")
+    with tempfile.TemporaryDirectory() as tmp:
+        W.write_fasta(os.path.join(tmp, "in.fa"), w.seqs, width=60)
+        W.write_fasta(os.path.join(tmp, "bg.fa"), bg_seqs, width=60)
+        if w.boxes:
+            W.write_boxes(os.path.join(tmp, "in.boxes"), w.boxes)
+        subprocess.run([ref_bin] + bg_args, cwd=tmp, check=True, capture_output=True)
+        b_args = fg_args + ["-b", "bg.motex", "-u", "un.motex"]
+        if kind == "b":
+            args = b_args + extra
+            outputs = ["out.motex", "un.motex"] + (["out.smile", "un.smile"] if "-U" in extra else [])
+            keep = ["in.fa", "bg.motex"] + (["in.boxes"] if w.boxes else [])
+        else:
+            # the unmatched motifs of a background run, searched in the background sequences
+            subprocess.run([ref_bin] + b_args, cwd=tmp, check=True, capture_output=True)
+            os.replace(os.path.join(tmp, "un.motex"), os.path.join(tmp, "fg.in"))
+            os.replace(os.path.join(tmp, "bg.fa"), os.path.join(tmp, "in.fa"))
+            args = list(fg_args)
+            args[args.index("-q") + 1] = "0"
+            args += ["-n", "0", "-I", "fg.in"] + extra
+            outputs = ["out.motex"]
+            keep = ["in.fa", "fg.in"]
+        for f in keep:
+            shutil.copy(os.path.join(tmp, f), d)
+        rc, ref_out = run_outputs(ref_bin, args, tmp, outputs)
+        rc2, port_out = run_outputs(PORT, args + ["-t", str(os.cpu_count())], tmp, outputs)
+    if rc != 0 or any(v is None for v in ref_out.values()):
+        sys.exit(f"make_golden: reference failed on {name} (rc={rc})")
+    if rc2 != rc or port_out != ref_out:
+        sys.exit(f"make_golden: oracle/_build/motex_port disagrees with the reference on {name}")
+    for o, text in ref_out.items():
+        with open(os.path.join(d, expected_name(o)), "w") as f:
+            f.write(text)
+    with open(os.path.join(d, "case.json"), "w") as f:
+        json.dump({"args": args, "reference": "motexCPU", "outputs": outputs}, f, indent=1)
+    print(f"{name:28s} kind={kind} " + " ".join(f"{o}={t.count(chr(10))}" for o, t in ref_out.items()) + " ok")
+
+
 def main():
     if not os.path.exists(os.path.join(REF, "motexCPU")):
         sys.exit("make_golden: oracle/_ref/motexCPU missing (run oracle/build_ref.sh on x86-64)")
@@ -261,6 +372,8 @@ def main():
                        "motifs": ref_out.count("\n") - ref_out.count("#") - 3}, f, indent=1)
         print(f"{name:28s} seqs={len(w.seqs) if raw is None else 'raw':>5} "
               f"lines={ref_out.count(chr(10)):6d} ok")
+    for case in mode_cases():
+        build_mode_case(*case)
 
 
 if __name__ == "__main__":

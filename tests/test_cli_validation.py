@@ -74,9 +74,3 @@ def test_option_combinations_match_oracle(native_built, oracle_port, name, extra
     o = run_cli(oracle_port, None, BASE + extra, files=files)
     assert g[0] == o[0] == 1
     assert g[2] == o[2] and "Error" in g[2]
-
-
-@pytest.mark.parametrize("extra", [["-b", "bg.motex", "-u", "un.txt"], ["-I", "un.in"]], ids=["background", "unmatched_in"])
-def test_background_modes_rejected(native_built, extra):
-    rc, out, err = run_cli(native_built.CLI_PATH, None, BASE + extra, files={"in.fa": FA})
-    assert rc == 1 and out is None and "not part of motexGPU" in err

@@ -14,8 +14,9 @@ import subprocess
 
 import pytest
 
-from conftest import ORACLE_DIR, PORT_LIB, ROOT, golden_cases
-from helpers import expected_smile, load_case, read_smile, run_cli
+from conftest import ORACLE_DIR, PORT_LIB, ROOT, golden_cases, mode_cases
+from helpers import (expected_smile, load_case, load_mode_case, read_smile, run_cli, run_outputs,
+                     same_but_pvalues)
 
 REFERENCE = "/root/reference"
 
@@ -38,12 +39,29 @@ def test_port_smile_matches_reference_golden(oracle_port, name):
     assert smile == expected_smile(name)
 
 
+@pytest.mark.parametrize("name", mode_cases())
+def test_port_modes_match_reference_golden(oracle_port, name):
+    """-b/-u/-S/-U and -I: every output file of the reference itself.  Built
+    on x86-64, as the fixtures were, the port's long double p-values match
+    to the last printed digit."""
+    d, args, expected = load_mode_case(name)
+    rc, got, err = run_outputs(oracle_port, d, args, list(expected), extra=["-t", "4"])
+    assert rc == 0, err
+    for o, text in expected.items():
+        if platform.machine() in ("x86_64", "AMD64"):
+            assert got[o] == text, o
+        else:
+            assert same_but_pvalues(got[o], text) is None, o
+
+
 def test_golden_set_is_complete():
     names = set(golden_cases())
     for needed in ("c1_dna_hd_64x500", "dna_ed_24seq", "prot_hd_20seq", "prot_ed_20seq", "struct_planted_hd",
                    "struct_planted_ed", "quorum_boundary_q29", "dna_with_N_ed", "short_seqs_ed",
                    "long_factor_k70_ed", "q0_n0_all_words", "caps_Q60_n2_N40"):
         assert needed in names
+    assert {"bg_dna_hd_smile", "bg_prot_ed", "bg_struct_hd_smile", "bg_struct2_ed", "fore_dna_hd",
+            "fore_prot_ed"} <= set(mode_cases())
     smile = {n for n in names if expected_smile(n) is not None}
     assert {"prot_hd_20seq", "usr_hd", "struct_planted_hd", "struct2_planted_ed"} <= smile
 

@@ -53,6 +53,7 @@ WORKLOADS = {
     "dna_long": lambda s: W.dna_long(scale=s),
     "structured_d1": lambda s: W.structured(scale=s, d=1),
     "structured_d0": lambda s: W.structured(scale=s, d=0),
+    "dna_satellite": lambda s: W.dna_satellite(scale=s),
 }
 DEFAULT_WORKLOAD = "dna_ed"
 # algorithmic integer operations per DP cell (one factor x one text position)
@@ -254,7 +255,7 @@ def batched_vs_plain(native, ctx, seed=3, sample=30, scale=1.0):
                     f"of the first {sample} sequences (host wall time, both)"}
 
 
-def serving(native, nreq=300, rate_hz=100.0, seed=5, max_batch=32, workers=2):
+def serving(native, nreq=2000, rate_hz=100.0, seed=5, max_batch=32, workers=2):
     """Poisson request stream through the continuous-batching server, and
     the same arrivals served one request at a time (plain per-request GPU
     path, FIFO).  Latency = completion - arrival."""
@@ -403,7 +404,7 @@ def run_gpu(args, rank, world, local_rank):
     extras = {}
     if rank == 0 and not args.no_extras and args.scale == 1.0:
         extras["batched_vs_plain"] = batched_vs_plain(native, ctx)
-        extras["serving"] = serving(native)
+        extras["serving"] = serving(native, nreq=args.serve_requests)
     out = {
         "metric": "GCUPS (reference DP cell updates per second), whole-set word-based motif extraction",
         "value": round(value, 2), "unit": "GCUPS", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
@@ -462,6 +463,8 @@ def main():
     ap.add_argument("--scale", type=float, default=1.0,
                     help="shrink the workload (profiling captures only; 1.0 = the benchmark size)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--serve-requests", type=int, default=2000,
+                    help="requests in the serving stream (Poisson arrivals, 100/s)")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the batched-vs-plain and serving sections")
     args = ap.parse_args()

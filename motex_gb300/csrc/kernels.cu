@@ -150,66 +150,190 @@ __global__ void k_presence ( const uint8_t * __restrict__ raw, uint64_t total, u
         if ( seen[i] ) present[i] = 1;
 }
 
-/*
- * One warp per 32-position block (grid-stride).  Lane r maps position
- * 32k+r to its symbol code, finds its sequence, and the warp forms the bit
- * planes, validity and end masks with ballots.  Also writes the position of
- * every factor end (in input order) to wpos.
- */
-__global__ void k_pack ( PackArgs a )
+// ------------------------------------------------------------ TMA staging
+
+namespace
 {
+
+constexpr uint32_t kStageWaitLimit = 1u << 22;   // try_wait polls before a staging wait gives up
+
+__device__ __forceinline__ uint32_t smem_u32 ( const void * p ) { return ( uint32_t ) __cvta_generic_to_shared ( p ); }
+
+__device__ __forceinline__ void mbar_init ( uint64_t * bar, uint32_t count )
+{
+    asm volatile ( "mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"( smem_u32 ( bar ) ), "r"( count ) : "memory" );
+}
+
+__device__ __forceinline__ void mbar_expect_tx ( uint64_t * bar, uint32_t bytes )
+{
+    asm volatile ( "mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"( smem_u32 ( bar ) ), "r"( bytes )
+                   : "memory" );
+}
+
+__device__ __forceinline__ bool mbar_try_wait ( uint64_t * bar, uint32_t parity )
+{
+    uint32_t done;
+    asm volatile ( "{\n\t.reg .pred p;\n\t"
+                   "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                   "selp.u32 %0, 1, 0, p;\n\t}"
+                   : "=r"( done )
+                   : "r"( smem_u32 ( bar ) ), "r"( parity )
+                   : "memory" );
+    return done != 0;
+}
+
+// Bounded wait for the completion of phase `parity`; false if it gave up.
+__device__ __forceinline__ bool mbar_wait_bounded ( uint64_t * bar, uint32_t parity )
+{
+    for ( uint32_t it = 0; it < kStageWaitLimit; ++it )
+        if ( mbar_try_wait ( bar, parity ) ) return true;
+    return false;
+}
+
+// One-dimensional TMA copy global -> shared, completing on `bar`.  Both
+// addresses 16-byte aligned, bytes a multiple of 16.
+__device__ __forceinline__ void bulk_copy_g2s ( void * dst, const void * src, uint32_t bytes, uint64_t * bar )
+{
+    asm volatile ( "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                       smem_u32 ( dst ) ),
+                   "l"( src ), "r"( bytes ), "r"( smem_u32 ( bar ) )
+                   : "memory" );
+}
+
+} // namespace
+
+/*
+ * Packing.  A persistent grid walks tiles of kPackTile raw bytes; each tile
+ * is staged into shared memory by one TMA bulk copy (double-buffered: the
+ * copy of the CTA's next tile runs while this one is packed).  Warp w of
+ * the CTA packs the tile's 32-position blocks 32w .. 32w+31: in step i,
+ * lane r takes position 32(k0+i)+r from shared memory (one conflict-free
+ * 32-byte row per step), writes its code and its factor-end entry (both
+ * coalesced), and the warp forms block k0+i's bit planes, validity and end
+ * masks by ballot; lane i keeps them, so every plane and mask row leaves as
+ * one coalesced 128-byte store per warp.
+ */
+__global__ void __launch_bounds__ ( kPackThreads ) k_pack ( PackArgs a )
+{
+    __shared__ __align__ ( 128 ) uint8_t stage[2][kPackTile];
+    __shared__ __align__ ( 8 ) uint64_t bar[2];
     __shared__ uint8_t cmap[256];
     for ( int i = threadIdx.x; i < 256; i += blockDim.x ) cmap[i] = a.cmap[i];
-    __syncthreads ();
-    const int lane = threadIdx.x & 31;
-    const uint32_t warps = ( gridDim.x * blockDim.x ) >> 5;
-    for ( uint32_t k = ( blockIdx.x * blockDim.x + threadIdx.x ) >> 5; k < a.nblk; k += warps )
+    const uint64_t ntiles = ( a.total + kPackTile - 1 ) / kPackTile;
+    if ( threadIdx.x == 0 )
     {
-        const uint64_t pos = ( uint64_t ) k * 32 + lane;
-        uint32_t code = 0;
-        bool valid = false, is_end = false;
+        mbar_init ( &bar[0], 1 );
+        mbar_init ( &bar[1], 1 );
+        asm volatile ( "fence.mbarrier_init.release.cluster;" ::: "memory" );
+    }
+    __syncthreads ();
+
+    auto issue = [&] ( uint64_t t, int buf ) {       // thread 0 only
+        const uint64_t start = t * kPackTile;
+        const uint64_t left = ( a.total - start + 15 ) & ~15ull;
+        const uint32_t bytes = left < kPackTile ? ( uint32_t ) left : kPackTile;
+        mbar_expect_tx ( &bar[buf], bytes );
+        bulk_copy_g2s ( stage[buf], a.raw + start, bytes, &bar[buf] );
+    };
+    // tile n of this CTA (n = 0, 1, ...) goes to buffer n & 1 and completes that
+    // buffer's barrier phase n >> 1
+    if ( blockIdx.x < ntiles && threadIdx.x == 0 ) issue ( blockIdx.x, 0 );
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t full = 0xffffffffu;
+    bool failed = false, next_issued = false;
+    uint32_t n = 0;
+    for ( uint64_t t = blockIdx.x; t < ntiles; t += gridDim.x, ++n )
+    {
+        const int buf = n & 1;
+        const uint64_t tn = t + gridDim.x;
+        next_issued = tn < ntiles;
+        if ( next_issued && threadIdx.x == 0 )
+        {
+            // the other buffer was last read before the barrier that ended the previous tile
+            asm volatile ( "fence.proxy.async.shared::cta;" ::: "memory" );
+            issue ( tn, buf ^ 1 );
+        }
+        const bool ok = mbar_wait_bounded ( &bar[buf], ( n >> 1 ) & 1 );
+        if ( __syncthreads_or ( ! ok ) )
+        {
+            failed = true;
+            break;
+        }
+
+        const uint64_t k0 = t * ( kPackTile / 32 ) + ( uint64_t ) warp * 32;     // first block of this warp
+        const uint8_t * row = stage[buf] + ( size_t ) warp * 32 * 32;
+        uint64_t pos = k0 * 32 + lane;
+        // sequence of this lane's first position: offs[s] <= pos < offs[s + 1]
+        uint32_t s = 0;
         if ( pos < a.total )
         {
-            // largest s with offs[s] <= pos (lane 0 searches, the rest walk forward)
-            uint32_t s = 0;
-            if ( lane == 0 )
+            uint32_t lo = 0, hi = a.nseq;
+            while ( hi - lo > 1 )
             {
-                uint32_t lo = 0, hi = a.nseq;                 // offs[lo] <= pos < offs[hi]
-                while ( hi - lo > 1 )
-                {
-                    uint32_t mid = ( lo + hi ) >> 1;
-                    if ( a.offs[mid] <= pos ) lo = mid; else hi = mid;
-                }
-                s = lo;
+                const uint32_t mid = ( lo + hi ) >> 1;
+                if ( a.offs[mid] <= pos ) lo = mid; else hi = mid;
             }
-            s = __shfl_sync ( __activemask (), s, 0 );
-            while ( a.offs[s + 1] <= pos ) ++s;
-            const uint64_t start = a.offs[s], end = a.offs[s + 1];
-            const uint64_t rel = pos - start;
-            const bool is_short = ( end - start ) < a.tml;
-            code = cmap[a.raw[pos]];
-            a.codes[pos] = ( uint8_t ) code;
-            // pattern mode: sequences below npat are patterns (factors
-            // only), the rest are texts (searched only)
-            valid = ! is_short && rel >= a.vstart && s >= a.npat;
-            is_end = pos == end - 1;
-            if ( ! is_short && rel + 1 >= a.l && ( a.npat == 0 || s < a.npat ) )
-                a.wpos[a.wstart[s] + ( uint32_t ) ( rel + 1 - a.l )] = ( uint32_t ) pos;
+            s = lo;
         }
-        const uint32_t full = 0xffffffffu;
+        uint64_t start = a.offs[s], end = a.offs[s + 1];
+        uint32_t ws = a.wstart[s];
+        uint32_t pl[kMaxPlanes] = {}, vm_mine = 0, em_mine = 0;
+#pragma unroll 4
+        for ( int i = 0; i < 32; ++i, pos += 32 )
+        {
+            uint32_t code = 0;
+            bool valid = false, is_end = false;
+            if ( pos < a.total )
+            {
+                while ( end <= pos )
+                {
+                    ++s;
+                    start = end;
+                    end = a.offs[s + 1];
+                    ws = a.wstart[s];
+                }
+                code = cmap[row[i * 32 + lane]];
+                a.codes[pos] = ( uint8_t ) code;
+                const uint64_t rel = pos - start;
+                const bool is_short = ( end - start ) < a.tml;
+                // pattern mode: sequences below npat are patterns (factors
+                // only), the rest are texts (searched only)
+                valid = ! is_short && rel >= a.vstart && s >= a.npat;
+                is_end = pos == end - 1;
+                if ( ! is_short && rel + 1 >= a.l && ( a.npat == 0 || s < a.npat ) )
+                    a.wpos[ws + ( uint32_t ) ( rel + 1 - a.l )] = ( uint32_t ) pos;
+            }
 #pragma unroll
-        for ( int b = 0; b < kMaxPlanes; ++b )
-        {
-            if ( b >= a.B ) break;
-            uint32_t pl = __ballot_sync ( full, ( code >> b ) & 1u );
-            if ( lane == 0 ) a.planes[( size_t ) b * a.plane_stride + k + 1] = pl;
+            for ( int b = 0; b < kMaxPlanes; ++b )
+            {
+                if ( b >= a.B ) break;
+                const uint32_t word = __ballot_sync ( full, ( code >> b ) & 1u );
+                if ( lane == i ) pl[b] = word;
+            }
+            const uint32_t vw = __ballot_sync ( full, valid ), ew = __ballot_sync ( full, is_end );
+            if ( lane == i )
+            {
+                vm_mine = vw;
+                em_mine = ew;
+            }
         }
-        uint32_t vm = __ballot_sync ( full, valid ), em = __ballot_sync ( full, is_end );
-        if ( lane == 0 )
+        const uint64_t k = k0 + lane;
+        if ( k < a.nblk )
         {
-            a.vmask[k] = vm;
-            a.emask[k] = em;
+#pragma unroll
+            for ( int b = 0; b < kMaxPlanes; ++b )
+                if ( b < a.B ) a.planes[( size_t ) b * a.plane_stride + k + 1] = pl[b];
+            a.vmask[k] = vm_mine;
+            a.emask[k] = em_mine;
         }
+        __syncthreads ();                            // this buffer may be refilled
+    }
+    if ( failed )
+    {
+        if ( threadIdx.x == 0 ) atomicExch ( a.err, 1u );
+        // let copies still in flight land before the CTA's shared memory goes away
+        mbar_wait_bounded ( &bar[n & 1], ( n >> 1 ) & 1 );
+        if ( next_issued ) mbar_wait_bounded ( &bar[( n + 1 ) & 1], ( ( n + 1 ) >> 1 ) & 1 );
     }
 }
 
@@ -316,18 +440,24 @@ __global__ void __launch_bounds__ ( kSortThreads ) k_radix_scatter ( const uint3
 }
 
 // head[i] = 1 iff the factor at idx[i] differs from the one at idx[i-1].
-__global__ void k_heads ( const uint32_t * __restrict__ idx, uint32_t n, const uint8_t * __restrict__ codes,
-                          uint32_t l, uint8_t * __restrict__ head )
+// keys[i] is the most significant key chunk of factor idx[i] (sorted order,
+// coalesced); when it is the whole factor (full_key) it decides alone,
+// otherwise equal chunks fall back to comparing the symbols.
+__global__ void k_heads ( const uint32_t * __restrict__ idx, const uint32_t * __restrict__ keys, int full_key,
+                          uint32_t n, const uint8_t * __restrict__ codes, uint32_t l, uint8_t * __restrict__ head )
 {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if ( i >= n ) return;
     uint8_t h = 1;
-    if ( i > 0 )
+    if ( i > 0 && keys[i] == keys[i - 1] )
     {
-        const uint32_t p = idx[i], q = idx[i - 1];
         h = 0;
-        for ( uint32_t e = 0; e < l; ++e )
-            if ( codes[p - e] != codes[q - e] ) { h = 1; break; }
+        if ( ! full_key )
+        {
+            const uint32_t p = idx[i], q = idx[i - 1];
+            for ( uint32_t e = 0; e < l; ++e )
+                if ( codes[p - e] != codes[q - e] ) { h = 1; break; }
+        }
     }
     head[i] = h;
 }

@@ -29,7 +29,11 @@ struct PackArgs
     uint32_t *       emask;
     uint32_t *       wpos;
     uint32_t         nblk;
+    uint32_t *       err;          // set to 1 if a staging wait gave up
 };
+
+constexpr int kPackThreads = 256;              // 8 warps, each packs 32 blocks of 32 positions
+constexpr uint32_t kPackTile = 8192;           // positions (raw bytes) per staged tile
 
 struct FinalizeArgs
 {
@@ -63,7 +67,8 @@ __global__ void k_gather_key ( const uint32_t * idx, uint32_t n, const uint8_t *
 __global__ void k_radix_hist ( const uint32_t * keys, uint32_t n, int shift, uint32_t * hist, uint32_t ntiles );
 __global__ void k_radix_scatter ( const uint32_t * keys_in, const uint32_t * vals_in, uint32_t * keys_out,
                                   uint32_t * vals_out, uint32_t n, int shift, const uint32_t * offsets, uint32_t ntiles );
-__global__ void k_heads ( const uint32_t * idx, uint32_t n, const uint8_t * codes, uint32_t l, uint8_t * head );
+__global__ void k_heads ( const uint32_t * idx, const uint32_t * keys, int full_key, uint32_t n, const uint8_t * codes,
+                          uint32_t l, uint8_t * head );
 __global__ void k_unique ( const uint32_t * idx, const uint8_t * head, const uint32_t * pref, uint32_t n,
                            uint32_t * uniq_pos );
 __global__ void k_wplanes32 ( const uint32_t * uniq_pos, uint32_t U, const uint8_t * codes, uint32_t l, uint32_t B,

@@ -72,13 +72,13 @@ enum Slot
     S_RAW, S_OFFS, S_WSTART, S_QOK, S_CMAP, S_PRESENT, S_CODES, S_PLANES, S_VMASK, S_EMASK,
     S_WPOS, S_KEY0, S_KEY1, S_IDX1, S_HIST, S_HEAD, S_PREF, S_UNIQ, S_WPL32, S_WPL64,
     S_CHUNKS, S_UACC, S_VACC, S_FLAGS, S_MARK, S_RECU, S_RECV, S_PREF2, S_RECS, S_TILES,
-    S_SCALAR, S_UOUT, S_VOUT, S_WPL0, S_WPL1, S_ROWOK, S_ROWEND, S_WPLN, S_SEQSTART, S_XOFF, S_COUNT
+    S_SCALAR, S_UOUT, S_VOUT, S_WPL0, S_WPL1, S_ROWOK, S_ROWEND, S_WPLN, S_SEQSTART, S_XOFF, S_HTILES, S_COUNT
 };
 
 // Pinned staging layout of a job (bytes).
 constexpr size_t kPinPresent = 0;          // 256 x u32 symbol presence
 constexpr size_t kPinCmap = 1024;          // 256 B symbol -> code
-constexpr size_t kPinScalar = 2048;        // u32 unique count, u32 motif count
+constexpr size_t kPinScalar = 2048;        // u32 unique count, u32 motif count, -, staging error flag
 constexpr size_t kPinXoff = 2560;          // structure offset table (<= 384 u32)
 constexpr size_t kPinChunks = 4096;        // chunk table
 constexpr size_t kPinStage = 65536;        // input upload / result download
@@ -332,18 +332,22 @@ int scan_flags ( Job * j, const uint8_t * in, uint32_t n, uint32_t * out, uint32
     return MOTEX_OK;
 }
 
-// Stable sort of the factor ends by their packed keys; result in *idx_out.
-int sort_factors ( Job * j, uint32_t n, uint32_t ** idx_out )
+// Stable sort of the factor ends by their packed keys; result in *idx_out,
+// the most significant 32-bit key chunk of every sorted factor in *keys_out
+// (the whole factor when l * B <= 32, *full_key).
+int sort_factors ( Job * j, uint32_t n, uint32_t ** idx_out, const uint32_t ** keys_out, bool * full_key )
 {
     const uint32_t l = j->prm.l, B = ( uint32_t ) j->B;
     const uint32_t bits = l * B;
     const uint32_t nchunk = ( bits + 31 ) / 32;
     const uint32_t ntiles = ( uint32_t ) blocks_for ( n, kSortTile );
-    uint32_t *key0, *key1, *idx1, *hist;
+    const uint32_t nhist = 256 * ntiles;
+    uint32_t *key0, *key1, *idx1, *hist, *tsum;
     MTX_TRY ( ensure ( j, S_KEY0, n, &key0 ) );
     MTX_TRY ( ensure ( j, S_KEY1, n, &key1 ) );
     MTX_TRY ( ensure ( j, S_IDX1, n, &idx1 ) );
-    MTX_TRY ( ensure ( j, S_HIST, ( size_t ) 256 * ntiles, &hist ) );
+    MTX_TRY ( ensure ( j, S_HIST, nhist, &hist ) );
+    MTX_TRY ( ensure ( j, S_HTILES, blocks_for ( nhist, kScanTile ), &tsum ) );
     uint32_t * idx0 = dptr<uint32_t> ( j, S_WPOS );
     uint32_t *kin = key0, *kout = key1, *iin = idx0, *iout = idx1;
     for ( uint32_t ch = 0; ch < nchunk; ++ch )
@@ -353,13 +357,19 @@ int sort_factors ( Job * j, uint32_t n, uint32_t ** idx_out )
         for ( uint32_t pass = 0; pass * 8 < cbits; ++pass )
         {
             MTX_LAUNCH ( k_radix_hist, ntiles, kSortThreads, kin, n, ( int ) ( 8 * pass ), hist, ntiles );
-            MTX_LAUNCH ( k_scan_single, 1, kScanThreads, hist, 256 * ntiles, ( uint32_t * ) nullptr );
+            // digit-major histogram -> scatter offsets, by the multi-CTA scan (in place)
+            cudaError_t e = scan_exclusive_u32 ( hist, nhist, hist, nullptr, tsum, j->ctx->st );
+            j->ctx->launches += 3;
+            j->launches += 3;
+            if ( e != cudaSuccess ) return fail ( MOTEX_ECUDA, "histogram scan failed: %s", cudaGetErrorString ( e ) );
             MTX_LAUNCH ( k_radix_scatter, ntiles, kSortThreads, kin, iin, kout, iout, n, ( int ) ( 8 * pass ), hist, ntiles );
             std::swap ( kin, kout );
             std::swap ( iin, iout );
         }
     }
     *idx_out = iin;
+    *keys_out = kin;
+    *full_key = nchunk == 1;
     return MOTEX_OK;
 }
 
@@ -644,21 +654,28 @@ int stage_pack ( Job * j, bool * need_sync )
     pa.emask = emask;
     pa.wpos = wpos;
     pa.nblk = j->nblk;
-    MTX_LAUNCH ( k_pack, std::min<unsigned> ( 16 * j->ctx->num_sms, blocks_for ( j->nblk, 8 ) ), 256, pa );
+    uint32_t * scalar;
+    MTX_TRY ( ensure ( j, S_SCALAR, 4, &scalar ) );
+    pa.err = scalar + 3;
+    MTX_CUDA ( cudaMemsetAsync ( scalar + 3, 0, 4, st ) );
+    // persistent: 8 CTAs per SM (the register and shared-memory budget allows
+    // it), each with two staged tiles in flight
+    const uint64_t ntiles = ( j->total + kPackTile - 1 ) / kPackTile;
+    MTX_LAUNCH ( k_pack, ( unsigned ) std::min<uint64_t> ( ntiles, 8ull * j->ctx->num_sms ), kPackThreads, pa );
 
     j->structured = P.nb_gaps > 0;
     j->generic = ! j->structured && P.l > 32;
-    uint32_t * scalar;
-    MTX_TRY ( ensure ( j, S_SCALAR, 4, &scalar ) );
     if ( ! j->structured && ! j->npat && j->nwords > 0 )
     {
         uint32_t * idx;
-        MTX_TRY ( sort_factors ( j, j->nwords, &idx ) );
+        const uint32_t * keys;
+        bool full_key;
+        MTX_TRY ( sort_factors ( j, j->nwords, &idx, &keys, &full_key ) );
         uint8_t * head;
         uint32_t * pref;
         MTX_TRY ( ensure ( j, S_HEAD, j->nwords, &head ) );
         MTX_TRY ( ensure ( j, S_PREF, j->nwords, &pref ) );
-        MTX_LAUNCH ( k_heads, blocks_for ( j->nwords, 256 ), 256, idx, j->nwords, codes, P.l, head );
+        MTX_LAUNCH ( k_heads, blocks_for ( j->nwords, 256 ), 256, idx, keys, ( int ) full_key, j->nwords, codes, P.l, head );
         MTX_TRY ( scan_flags ( j, head, j->nwords, pref, scalar ) );
         MTX_CUDA ( cudaMemcpyAsync ( pin<uint32_t> ( j, kPinScalar ), scalar, 4, cudaMemcpyDeviceToHost, st ) );
         j->uniq = idx;                               // sorted factor ends; compacted in stage_plan
@@ -1080,6 +1097,9 @@ int stage_finalize ( Job * j, bool * need_sync )
 
 int stage_compact ( Job * j )
 {
+    // the packer's staging-wait flag comes back with the results
+    MTX_CUDA ( cudaMemcpyAsync ( pin<uint32_t> ( j, kPinScalar ) + 3, dptr<uint32_t> ( j, S_SCALAR ) + 3, 4,
+                                 cudaMemcpyDeviceToHost, j->ctx->st ) );
     if ( ! j->npat )
     {
         if ( ! j->replaying ) j->nrec = pin<uint32_t> ( j, kPinScalar )[1];
@@ -1096,6 +1116,8 @@ int stage_compact ( Job * j )
 int read_times ( Job * j )
 {
     MTX_CUDA ( cudaEventSynchronize ( j->ev1 ) );
+    if ( pin<uint32_t> ( j, kPinScalar )[3] )
+        return fail ( MOTEX_ECUDA, "packing: a TMA staging wait gave up (copy not completed)" );
     MTX_CUDA ( cudaEventElapsedTime ( &j->device_ms, j->ev0, j->ev1 ) );
     if ( j->dp_timed ) MTX_CUDA ( cudaEventElapsedTime ( &j->dp_ms, j->evd0, j->evd1 ) );
     return MOTEX_OK;

@@ -179,6 +179,23 @@ def dna_long(seed: int = 4, scale: float = 1.0) -> Workload:
     return Workload("dna_long", "DNA", seqs, d=0, k=20, e=3, q=50)
 
 
+def dna_satellite(seed: int = 6, scale: float = 1.0) -> Workload:
+    """Satellite-like DNA: 64 sequences of ~1 Mnt, each an exact tandem copy
+    of one random 4096-nt unit from a random phase.  Only ~4k distinct words
+    exist, so the DP is short and the HBM-bound stages (packing, the dedup
+    sort of every factor, scans, compaction) carry a real share of the run:
+    the workload their bandwidth is measured on."""
+    rng = np.random.default_rng(seed)
+    unit = _rand_seq(rng, DNA, 4096)
+    length = max(8192, int(1_000_000 * scale))
+    reps = length // len(unit) + 2
+    seqs = []
+    for _ in range(64):
+        a = int(rng.integers(len(unit)))
+        seqs.append((unit * reps)[a:a + length])
+    return Workload("dna_satellite", "DNA", seqs, d=0, k=12, e=1, q=50)
+
+
 def structured(seed: int = 2, scale: float = 1.0, d: int = 1) -> Workload:
     w = dna_ed(seed, scale, d=d)
     w.name = "structured"

@@ -205,6 +205,158 @@ __global__ void __launch_bounds__ ( kDPThreads ) k_dp_struct1 ( const StructArgs
 }
 
 /*
+ * Hamming, one gap, block by block.  Same ownership as k_dp_struct1 (a warp
+ * owns 32 box-0 rows and the 32+G-1 box-1 rows they need), but per block of
+ * 32 text positions each lane first forms three hit masks -- its box-0 row
+ * (valid ends only) and its two box-1 rows -- with no exchange, and box-0
+ * hits join a 64-bit history word (bits 0-31 the previous block, 32-63 this
+ * one).  Then one warp-uniform pass visits, in position order, only the
+ * positions where some lane's box-1 row hits (OR-reduced over the warp) or
+ * a sequence ends: the ballots, the gap window of box-0 ends behind the hit
+ * (popc of the history word at gmin+b1 .. gmax+b1 behind it) and the
+ * per-structure counts are those of k_dp_struct1; a sequence end flushes
+ * and clears the history up to it.
+ */
+template <int B>
+__global__ void __launch_bounds__ ( kDPThreads ) k_dp_struct1_hd ( const StructArgs a )
+{
+    extern __shared__ uint32_t smem[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t G = a.G;
+    uint32_t * s_cnt = smem + ( size_t ) threadIdx.x * G * 3;
+    uint32_t * s_u = s_cnt + G;
+    uint32_t * s_v = s_u + G;
+    for ( uint32_t k = 0; k < G; ++k ) s_cnt[k] = s_u[k] = s_v[k] = 0;
+
+    const uint32_t P0 = ( blockIdx.x * ( kDPThreads / 32 ) + warp ) * 32;
+    const uint32_t jx = P0 + lane;
+    const uint32_t r0 = P0 + a.gmin + a.b1 + lane;
+    const uint32_t r1 = r0 + 32;
+    const bool has_r1 = lane + 1 < ( int ) G;
+
+    uint32_t w0[B], w1a[B], w1b[B];
+#pragma unroll
+    for ( int b = 0; b < B; ++b )
+    {
+        w0[b] = jx < a.total ? a.wpl0[( size_t ) b * a.total + jx] : 0u;
+        w1a[b] = r0 < a.total ? a.wpl1[( size_t ) b * a.total + r0] : 0u;
+        w1b[b] = ( has_r1 && r1 < a.total ) ? a.wpl1[( size_t ) b * a.total + r1] : 0u;
+    }
+    uint32_t kvalid = 0;
+    if ( jx < a.total && a.row_ok[jx] )
+    {
+        const uint32_t xend = a.row_end[jx];
+        for ( uint32_t k = 0; k < G; ++k )
+            if ( jx + a.gmin + k + a.b1 < xend ) kvalid |= 1u << k;
+    }
+    const uint32_t Gmask = G >= 32 ? 0xffffffffu : ( ( 1u << G ) - 1u );
+    const uint32_t lo = a.gmin + a.b1, hi = a.gmax + a.b1;            // hi <= 31 (launch check)
+    const uint32_t wmask = hi - lo + 1 >= 32 ? 0xffffffffu : ( ( 1u << ( hi - lo + 1 ) ) - 1u );
+
+    const ChunkInfo ch = a.chunks[blockIdx.y];
+    int cur_split = ch.first_split;
+    const uint32_t * __restrict__ planes = a.text.planes;
+    const uint32_t stride = a.text.plane_stride;
+    const uint32_t l0 = a.l0, l1 = a.l1;
+    const uint32_t top0 = l0 >= 32 ? 0xffffffffu : ~( ( 1u << ( 32 - l0 ) ) - 1u );
+    const uint32_t top1 = l1 >= 32 ? 0xffffffffu : ~( ( 1u << ( 32 - l1 ) ) - 1u );
+    const uint32_t full = 0xffffffffu;
+
+    auto flush = [&] () {
+        for ( uint32_t k = 0; k < G; ++k )
+        {
+            const uint32_t c = s_cnt[k];
+            if ( ! c ) continue;
+            if ( cur_split < 0 ) s_u[k] += 1;
+            else if ( jx < a.total ) a.split_flags[( ( size_t ) cur_split * a.total + jx ) * G + k] = 1;
+            s_v[k] += c;
+            s_cnt[k] = 0;
+        }
+    };
+
+    uint64_t X = 0;
+    uint32_t prev[B];
+#pragma unroll
+    for ( int b = 0; b < B; ++b ) prev[b] = __ldg ( planes + ( size_t ) b * stride + ch.warm );
+    for ( uint32_t kb = ch.warm; kb < ch.end; ++kb )
+    {
+        uint32_t cur[B];
+#pragma unroll
+        for ( int b = 0; b < B; ++b ) cur[b] = __ldg ( planes + ( size_t ) b * stride + kb + 1 );
+        const uint32_t vm = __ldg ( a.text.vmask + kb ), em = __ldg ( a.text.emask + kb );
+        const bool counting = kb >= ch.begin;
+        uint32_t m0 = 0, ma = 0, mb = 0;
+#pragma unroll 8
+        for ( int r = 0; r < 32; ++r )
+        {
+            uint32_t Y[B];
+#pragma unroll
+            for ( int b = 0; b < B; ++b ) Y[b] = __funnelshift_rc ( prev[b], cur[b], r + 1 );
+            m0 |= ( uint32_t ) hd_hit<B> ( w0, Y, top0, a.e0 ) << r;
+            ma |= ( uint32_t ) hd_hit<B> ( w1a, Y, top1, a.e1 ) << r;
+            mb |= ( uint32_t ) hd_hit<B> ( w1b, Y, top1, a.e1 ) << r;
+        }
+        if ( ! has_r1 ) mb = 0;
+        X = ( ( uint64_t ) ( m0 & vm ) << 32 ) | ( X >> 32 );
+        // positions where some lane's box-1 row hits: OR over the warp by a
+        // shuffle butterfly (the redux form failed the parity tests here)
+        uint32_t R = ma | mb;
+#pragma unroll
+        for ( int o = 16; o; o >>= 1 ) R |= __shfl_xor_sync ( full, R, o );
+        if ( ! counting ) R = 0;
+        uint32_t E = em;
+        while ( R | E )
+        {
+            const int r = __ffs ( R | E ) - 1;
+            const uint32_t bit = 1u << r;
+            if ( R & bit )
+            {
+                const uint32_t Ha = __ballot_sync ( full, ( ma >> r ) & 1u ), Hb = __ballot_sync ( full, ( mb >> r ) & 1u );
+                const uint64_t H = ( ( uint64_t ) Hb << 32 ) | Ha;
+                const uint32_t g = ( uint32_t ) ( H >> lane ) & Gmask & kvalid;
+                if ( g )
+                {
+                    const uint32_t c = __popc ( ( uint32_t ) ( X >> ( 32 + r - hi ) ) & wmask );
+                    if ( c )
+                        for ( uint32_t k = 0; k < G; ++k )
+                            if ( ( g >> k ) & 1u ) s_cnt[k] += c;
+                }
+            }
+            if ( E & bit )
+            {
+                if ( counting )
+                {
+                    flush ();
+                    cur_split = -1;
+                }
+                X &= ~( ( 2ull << ( 32 + r ) ) - 1ull );          // box-0 ends of the finished sequence
+            }
+            R &= ~bit;
+            E &= ~bit;
+        }
+#pragma unroll
+        for ( int b = 0; b < B; ++b ) prev[b] = cur[b];
+    }
+    for ( uint32_t k = 0; k < G; ++k )
+    {
+        const uint32_t c = s_cnt[k];
+        if ( c )
+        {
+            if ( ch.last_split >= 0 && jx < a.total )
+                a.split_flags[( ( size_t ) ch.last_split * a.total + jx ) * G + k] = 1;
+            else
+                s_u[k] += 1;
+            s_v[k] += c;
+        }
+        if ( jx < a.total && ( s_u[k] | s_v[k] ) )
+        {
+            atomicAdd ( a.u_acc + ( size_t ) jx * G + k, s_u[k] );
+            atomicAdd ( a.v_acc + ( size_t ) jx * G + k, s_v[k] );
+        }
+    }
+}
+
+/*
  * Edit distance with the lane's three rows -- box 0 (length l0) and its two
  * box-1 rows (length b1) -- packed in one 32-bit register: SWAR lanes of
  * different lengths at offsets 0, oB = l0+1, oC = oB+b1+1, a guard bit above
@@ -380,14 +532,179 @@ __global__ void __launch_bounds__ ( kDPThreads ) k_dp_struct1_swar ( const Struc
     }
 }
 
+/*
+ * Packed edit distance (as k_dp_struct1_swar), block by block like
+ * k_dp_struct1_hd: phase 1 runs the packed Myers step over the 32 positions
+ * of a block and appends each lane's hit bit to its mask (box 0, row r0,
+ * row r1; the lanes' top bits are ordered, so one shift and one funnel shift
+ * append each), with the Myers state reset at sequence ends; phase 2 visits
+ * only the positions where a box-1 row hits or a sequence ends.
+ */
+template <int B>
+__global__ void __launch_bounds__ ( kDPThreads ) k_dp_struct1_swar_blk ( const StructArgs a, const HSwarConst C )
+{
+    extern __shared__ uint32_t smem[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t G = a.G;
+    uint32_t * s_cnt = smem + ( size_t ) threadIdx.x * G * 3;
+    uint32_t * s_u = s_cnt + G;
+    uint32_t * s_v = s_u + G;
+    for ( uint32_t k = 0; k < G; ++k ) s_cnt[k] = s_u[k] = s_v[k] = 0;
+
+    const uint32_t P0 = ( blockIdx.x * ( kDPThreads / 32 ) + warp ) * 32;
+    const uint32_t jx = P0 + lane;
+    const uint32_t r0 = P0 + a.gmin + a.b1 + lane;
+    const uint32_t r1 = r0 + 32;
+    const bool has_r1 = lane + 1 < ( int ) G;
+    uint32_t w[B];
+#pragma unroll
+    for ( int b = 0; b < B; ++b )
+    {
+        const uint32_t x0 = jx < a.total ? a.wpl0[( size_t ) b * a.total + jx] : 0u;
+        const uint32_t x1 = r0 < a.total ? a.wpl1[( size_t ) b * a.total + r0] : 0u;
+        const uint32_t x2 = ( has_r1 && r1 < a.total ) ? a.wpl1[( size_t ) b * a.total + r1] : 0u;
+        w[b] = x0 | ( x1 << C.oB ) | ( x2 << C.oC );
+    }
+    uint32_t kvalid = 0;
+    if ( jx < a.total && a.row_ok[jx] )
+    {
+        const uint32_t xend = a.row_end[jx];
+        for ( uint32_t k = 0; k < G; ++k )
+            if ( jx + a.gmin + k + a.b1 < xend ) kvalid |= 1u << k;
+    }
+    const uint32_t Gmask = G >= 32 ? 0xffffffffu : ( ( 1u << G ) - 1u );
+    const uint32_t lo = a.gmin + a.b1, hi = a.gmax + a.b1;            // hi <= 31 (launch check)
+    const uint32_t wmask = hi - lo + 1 >= 32 ? 0xffffffffu : ( ( 1u << ( hi - lo + 1 ) ) - 1u );
+    // bit positions of the three lanes' top bits: box 0 < row r0 < row r1
+    const uint32_t pA = __ffs ( C.bitA ) - 1, pB = __ffs ( C.bitB ) - 1, pC = __ffs ( C.bitC ) - 1;
+    const ChunkInfo ch = a.chunks[blockIdx.y];
+    int cur_split = ch.first_split;
+    const uint32_t * __restrict__ planes = a.text.planes;
+    const uint32_t stride = a.text.plane_stride;
+    const uint32_t sh = C.s;
+    const uint32_t full = 0xffffffffu;
+    uint32_t Pv = C.NG, Mv = 0, sc = C.SC0;
+    uint64_t X = 0;
+
+    auto flush = [&] () {
+        for ( uint32_t k = 0; k < G; ++k )
+        {
+            const uint32_t c = s_cnt[k];
+            if ( ! c ) continue;
+            if ( cur_split < 0 ) s_u[k] += 1;
+            else if ( jx < a.total ) a.split_flags[( ( size_t ) cur_split * a.total + jx ) * G + k] = 1;
+            s_v[k] += c;
+            s_cnt[k] = 0;
+        }
+    };
+
+    for ( uint32_t kb = ch.warm; kb < ch.end; ++kb )
+    {
+        uint32_t cur[B];
+#pragma unroll
+        for ( int b = 0; b < B; ++b ) cur[b] = __ldg ( planes + ( size_t ) b * stride + kb + 1 );
+        const uint32_t vm = __ldg ( a.text.vmask + kb ), em = __ldg ( a.text.emask + kb );
+        const bool counting = kb >= ch.begin;
+        uint32_t m0 = 0, ma = 0, mb = 0;
+#pragma unroll 4
+        for ( int r = 0; r < 32; ++r )
+        {
+            uint32_t x = 0;
+#pragma unroll
+            for ( int b = 0; b < B; ++b ) x |= w[b] ^ ( ( 0u - ( ( cur[b] >> r ) & 1u ) ) & C.NG );
+            const uint32_t Xv = ~x | Mv;
+            const uint32_t s1 = ( ~x & Pv ) + Pv;
+            const uint32_t Xh = ( s1 ^ Pv ) | ~x;
+            const uint32_t Ph = Mv | ~( Xh | Pv );
+            const uint32_t Mhs = Pv & Xh & C.NGm1;
+            const uint32_t mh = Pv & Xh & C.HB;
+            const uint32_t ph = Ph & C.HB;
+            sc = sc + ( ph >> sh ) - ( mh >> sh );
+            const uint32_t Ph2 = Ph << 1, Mh2 = Mhs << 1;
+            Pv = Mh2 | ~( Xv | Ph2 );
+            Mv = Ph2 & Xv & C.NG;
+            const uint32_t hits = ~( sc + C.K ) & C.HB;
+            // append bit 0 of (hits >> p) at bit 31; after 32 positions bit r is position r
+            m0 = __funnelshift_r ( m0, hits >> pA, 1 );
+            ma = __funnelshift_r ( ma, hits >> pB, 1 );
+            mb = __funnelshift_r ( mb, hits >> pC, 1 );
+            if ( ( em >> r ) & 1u )
+            {
+                Pv = C.NG;
+                Mv = 0;
+                sc = C.SC0;
+            }
+        }
+        if ( ! has_r1 ) mb = 0;
+        X = ( ( uint64_t ) ( m0 & vm ) << 32 ) | ( X >> 32 );
+        uint32_t R = ma | mb;
+#pragma unroll
+        for ( int o = 16; o; o >>= 1 ) R |= __shfl_xor_sync ( full, R, o );
+        if ( ! counting ) R = 0;
+        uint32_t E = em;
+        while ( R | E )
+        {
+            const int r = __ffs ( R | E ) - 1;
+            const uint32_t bit = 1u << r;
+            if ( R & bit )
+            {
+                const uint32_t Ha = __ballot_sync ( full, ( ma >> r ) & 1u ), Hb = __ballot_sync ( full, ( mb >> r ) & 1u );
+                const uint64_t H = ( ( uint64_t ) Hb << 32 ) | Ha;
+                const uint32_t g = ( uint32_t ) ( H >> lane ) & Gmask & kvalid;
+                if ( g )
+                {
+                    const uint32_t c = __popc ( ( uint32_t ) ( X >> ( 32 + r - hi ) ) & wmask );
+                    if ( c )
+                        for ( uint32_t k = 0; k < G; ++k )
+                            if ( ( g >> k ) & 1u ) s_cnt[k] += c;
+                }
+            }
+            if ( E & bit )
+            {
+                if ( counting )
+                {
+                    flush ();
+                    cur_split = -1;
+                }
+                X &= ~( ( 2ull << ( 32 + r ) ) - 1ull );
+            }
+            R &= ~bit;
+            E &= ~bit;
+        }
+    }
+    for ( uint32_t k = 0; k < G; ++k )
+    {
+        const uint32_t c = s_cnt[k];
+        if ( c )
+        {
+            if ( ch.last_split >= 0 && jx < a.total )
+                a.split_flags[( ( size_t ) ch.last_split * a.total + jx ) * G + k] = 1;
+            else
+                s_u[k] += 1;
+            s_v[k] += c;
+        }
+        if ( jx < a.total && ( s_u[k] | s_v[k] ) )
+        {
+            atomicAdd ( a.u_acc + ( size_t ) jx * G + k, s_u[k] );
+            atomicAdd ( a.v_acc + ( size_t ) jx * G + k, s_v[k] );
+        }
+    }
+}
+
 template <int B>
 static void launch_struct_b ( const StructArgs & a, bool ed, dim3 grid, size_t smem, cudaStream_t st )
 {
     HSwarConst C;
+    const bool block = ! getenv ( "MOTEX_STRUCT_NO_BLOCK" );
     if ( ed && ! getenv ( "MOTEX_STRUCT_NO_SWAR" ) && hswar_shape ( a, &C ) )
-        k_dp_struct1_swar<B><<<grid, kDPThreads, smem, st>>> ( a, C );
+    {
+        if ( block ) k_dp_struct1_swar_blk<B><<<grid, kDPThreads, smem, st>>> ( a, C );
+        else k_dp_struct1_swar<B><<<grid, kDPThreads, smem, st>>> ( a, C );
+    }
     else if ( ed )
         k_dp_struct1<B, true><<<grid, kDPThreads, smem, st>>> ( a );
+    else if ( block )
+        k_dp_struct1_hd<B><<<grid, kDPThreads, smem, st>>> ( a );
     else
         k_dp_struct1<B, false><<<grid, kDPThreads, smem, st>>> ( a );
 }

@@ -200,7 +200,7 @@ int swar_lanes ( uint32_t l )
 template <int B, int NL, int W>
 static bool launch_swar_bnw ( const DPArgs & a, const SwarConst & C, int UR, dim3 grid, cudaStream_t st )
 {
-    const size_t smem = ( size_t ) 3 * W * NL * kDPThreads * sizeof ( uint32_t );
+    const size_t smem = swar_smem_bytes ( B, NL, W );
     switch ( UR )
     {
         case 4:

@@ -280,6 +280,19 @@ __device__ __forceinline__ bool next_item ( const WorkItem * items, uint32_t nit
  * counted in per-lane fields and moved to shared memory every 32 positions.
  */
 
+/*
+ * Shared memory of the SWAR body: hit counters [field][thread] (count in the
+ * current text, texts seen, occurrences) and, for B <= 3, the per-thread
+ * match table Eq[code][register][thread]: the Myers Eq vector of each of the
+ * thread's W registers against each symbol code, so a step reads Eq with one
+ * shared-memory load (LSU pipe) instead of forming it from the bit planes.
+ */
+__host__ __device__ constexpr bool swar_table ( int B ) { return B <= 3; }
+__host__ __device__ constexpr size_t swar_smem_bytes ( int B, int NL, int W )
+{
+    return ( ( size_t ) 3 * W * NL + ( swar_table ( B ) ? ( size_t ) ( 1 << B ) * W : 0 ) ) * kDPThreads * sizeof ( uint32_t );
+}
+
 template <int B, int NL, int W, int UR>
 __device__ __forceinline__ void dp_swar_body ( const DPArgs & a, const SwarConst & C, uint32_t tile, uint32_t chunk )
 {
@@ -313,19 +326,31 @@ __device__ __forceinline__ void dp_swar_body ( const DPArgs & a, const SwarConst
     uint32_t Pv[W], Mv[W], sc[W], cnt[W];
 #pragma unroll
     for ( int i = 0; i < W; ++i ) { Pv[i] = C.NG; Mv[i] = 0; sc[i] = C.SC0; cnt[i] = 0; }
+    constexpr bool TAB = swar_table ( B );
+    uint32_t * s_eq = smem + 3 * NF * kDPThreads;            // [code][register][thread]
+    if constexpr ( TAB )
+    {
+        // text bits are cleared at the guards, so Eq is 1 there (lanes stay apart)
+        for ( int c = 0; c < ( 1 << B ); ++c )
+#pragma unroll
+            for ( int i = 0; i < W; ++i )
+            {
+                uint32_t x = 0;
+#pragma unroll
+                for ( int b = 0; b < B; ++b ) x |= wp[i][b] ^ ( ( ( c >> b ) & 1 ) ? C.NG : 0u );
+                s_eq[( c * W + i ) * kDPThreads + tid] = ~x;
+            }
+    }
 
     const ChunkInfo ch = a.chunks[chunk];
     int cur_split = ch.first_split;
     const uint32_t * __restrict__ planes = a.text.planes;
     const uint32_t stride = a.text.plane_stride;
 
-    auto step = [&] ( int i, const uint32_t ( &T )[B] ) {
-        uint32_t x = wp[i][0] ^ T[0];
-#pragma unroll
-        for ( int b = 1; b < B; ++b ) x |= wp[i][b] ^ T[b];
-        const uint32_t Xv = ~x | Mv[i];
-        const uint32_t s = ( ~x & Pv[i] ) + Pv[i];
-        const uint32_t Xh = ( s ^ Pv[i] ) | ~x;
+    auto step_eq = [&] ( int i, const uint32_t Eq ) {
+        const uint32_t Xv = Eq | Mv[i];
+        const uint32_t s = ( Eq & Pv[i] ) + Pv[i];
+        const uint32_t Xh = ( s ^ Pv[i] ) | Eq;
         const uint32_t Ph = Mv[i] | ~( Xh | Pv[i] );
         const uint32_t Mhs = Pv[i] & Xh & C.NGm1;
         const uint32_t mh = Pv[i] & Xh & C.HB;
@@ -334,6 +359,19 @@ __device__ __forceinline__ void dp_swar_body ( const DPArgs & a, const SwarConst
         const uint32_t Ph2 = Ph << 1, Mh2 = Mhs << 1;
         Pv[i] = Mh2 | ~( Xv | Ph2 );
         Mv[i] = Ph2 & Xv & C.NG;
+    };
+    auto step = [&] ( int i, const uint32_t ( &T )[B] ) {
+        uint32_t x = wp[i][0] ^ T[0];
+#pragma unroll
+        for ( int b = 1; b < B; ++b ) x |= wp[i][b] ^ T[b];
+        step_eq ( i, ~x );
+    };
+    // code of text position r from the plane words (bit b of the code in plane b)
+    auto code_at = [&] ( const uint32_t ( &pw )[B], int r ) {
+        uint32_t c = 0;
+#pragma unroll
+        for ( int b = 0; b < B; ++b ) c |= ( ( pw[b] >> r ) & 1u ) << b;
+        return c;
     };
     auto count = [&] ( int i ) { cnt[i] += ( ~( sc[i] + C.K ) & C.HB ) >> sh; };
     auto drain = [&] () {                           // register fields -> shared counters
@@ -379,14 +417,27 @@ __device__ __forceinline__ void dp_swar_body ( const DPArgs & a, const SwarConst
 #pragma unroll
                 for ( int rr = 0; rr < UR; ++rr )
                 {
-                    uint32_t T[B];
-#pragma unroll
-                    for ( int b = 0; b < B; ++b ) T[b] = ( 0u - ( ( cg[b] >> rr ) & 1u ) ) & C.NG;
-#pragma unroll
-                    for ( int i = 0; i < W; ++i )
+                    if constexpr ( TAB )
                     {
-                        step ( i, T );
-                        count ( i );
+                        const uint32_t * row = s_eq + code_at ( cg, rr ) * ( W * kDPThreads ) + tid;
+#pragma unroll
+                        for ( int i = 0; i < W; ++i )
+                        {
+                            step_eq ( i, row[i * kDPThreads] );
+                            count ( i );
+                        }
+                    }
+                    else
+                    {
+                        uint32_t T[B];
+#pragma unroll
+                        for ( int b = 0; b < B; ++b ) T[b] = ( 0u - ( ( cg[b] >> rr ) & 1u ) ) & C.NG;
+#pragma unroll
+                        for ( int i = 0; i < W; ++i )
+                        {
+                            step ( i, T );
+                            count ( i );
+                        }
                     }
                 }
             }
@@ -395,15 +446,28 @@ __device__ __forceinline__ void dp_swar_body ( const DPArgs & a, const SwarConst
         {
             for ( int r = 0; r < 32; ++r )
             {
-                uint32_t T[B];
-#pragma unroll
-                for ( int b = 0; b < B; ++b ) T[b] = ( 0u - ( ( cur[b] >> r ) & 1u ) ) & C.NG;
                 const bool count_here = counting && ( ( vm >> r ) & 1u );
-#pragma unroll
-                for ( int i = 0; i < W; ++i )
+                if constexpr ( TAB )
                 {
-                    step ( i, T );
-                    if ( count_here ) count ( i );
+                    const uint32_t * row = s_eq + code_at ( cur, r ) * ( W * kDPThreads ) + tid;
+#pragma unroll
+                    for ( int i = 0; i < W; ++i )
+                    {
+                        step_eq ( i, row[i * kDPThreads] );
+                        if ( count_here ) count ( i );
+                    }
+                }
+                else
+                {
+                    uint32_t T[B];
+#pragma unroll
+                    for ( int b = 0; b < B; ++b ) T[b] = ( 0u - ( ( cur[b] >> r ) & 1u ) ) & C.NG;
+#pragma unroll
+                    for ( int i = 0; i < W; ++i )
+                    {
+                        step ( i, T );
+                        if ( count_here ) count ( i );
+                    }
                 }
                 if ( ( em >> r ) & 1u )
                 {

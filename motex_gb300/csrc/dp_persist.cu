@@ -63,7 +63,7 @@ bool launch_b ( const JobDesc * jobs, const WorkItem * items, uint32_t nitems, u
 #define MTX_SWAR_P( NLV )                                                                                   \
     case NLV:                                                                                               \
     {                                                                                                       \
-        const size_t smem = ( size_t ) 3 * W * NLV * kDPThreads * sizeof ( uint32_t );                      \
+        const size_t smem = swar_smem_bytes ( B, NLV, W );                                                  \
         if ( occ ) { *occ = ctas_per_sm ( k_dp_swar_persist<B, NLV, W, 8>, smem ); return true; }            \
         cudaFuncSetAttribute ( k_dp_swar_persist<B, NLV, W, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize,   \
                                ( int ) smem );                                                              \

@@ -178,7 +178,7 @@ bool launch_dp_persistent ( const JobDesc * jobs, const WorkItem * items, uint32
 int persistent_ctas_per_sm ( int B, bool ed, bool scaled, int NL, int W, int UR );
 
 // Edit distance, NL = swar_lanes(l) >= 2 factors per 32-bit register (l <= 15);
-// dynamic shared memory 3 * W * NL * kDPThreads words.
+// dynamic shared memory swar_smem_bytes ( B, NL, W ).
 int swar_lanes ( uint32_t l );
 bool launch_dp_swar_ed ( const DPArgs & a, int B, int NL, int W, int UR, dim3 grid, cudaStream_t st );
 bool launch_dp_generic ( const DPArgs & a, int B, uint32_t nw64, bool ed, dim3 grid, cudaStream_t st );

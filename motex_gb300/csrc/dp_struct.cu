@@ -535,7 +535,8 @@ __global__ void __launch_bounds__ ( kDPThreads ) k_dp_struct1_swar ( const Struc
 /*
  * Packed edit distance (as k_dp_struct1_swar), block by block like
  * k_dp_struct1_hd: phase 1 runs the packed Myers step over the 32 positions
- * of a block and appends each lane's hit bit to its mask (box 0, row r0,
+ * of a block, with Eq read from a per-thread table by symbol code (shared
+ * memory after the counters), and appends each lane's hit bit to its mask (box 0, row r0,
  * row r1; the lanes' top bits are ordered, so one shift and one funnel shift
  * append each), with the Myers state reset at sequence ends; phase 2 visits
  * only the positions where a box-1 row hits or a sequence ends.
@@ -564,6 +565,16 @@ __global__ void __launch_bounds__ ( kDPThreads ) k_dp_struct1_swar_blk ( const S
         const uint32_t x1 = r0 < a.total ? a.wpl1[( size_t ) b * a.total + r0] : 0u;
         const uint32_t x2 = ( has_r1 && r1 < a.total ) ? a.wpl1[( size_t ) b * a.total + r1] : 0u;
         w[b] = x0 | ( x1 << C.oB ) | ( x2 << C.oC );
+    }
+    // Myers Eq of the packed register against every symbol code (text bits
+    // cleared at the guards, so Eq is 1 there): one shared load per position
+    uint32_t * s_eq = smem + ( size_t ) kDPThreads * G * 3;          // [code][thread]
+    for ( int c = 0; c < ( 1 << B ); ++c )
+    {
+        uint32_t x = 0;
+#pragma unroll
+        for ( int b = 0; b < B; ++b ) x |= w[b] ^ ( ( ( c >> b ) & 1 ) ? C.NG : 0u );
+        s_eq[c * kDPThreads + threadIdx.x] = ~x;
     }
     uint32_t kvalid = 0;
     if ( jx < a.total && a.row_ok[jx] )
@@ -609,12 +620,13 @@ __global__ void __launch_bounds__ ( kDPThreads ) k_dp_struct1_swar_blk ( const S
 #pragma unroll 4
         for ( int r = 0; r < 32; ++r )
         {
-            uint32_t x = 0;
+            uint32_t c = 0;
 #pragma unroll
-            for ( int b = 0; b < B; ++b ) x |= w[b] ^ ( ( 0u - ( ( cur[b] >> r ) & 1u ) ) & C.NG );
-            const uint32_t Xv = ~x | Mv;
-            const uint32_t s1 = ( ~x & Pv ) + Pv;
-            const uint32_t Xh = ( s1 ^ Pv ) | ~x;
+            for ( int b = 0; b < B; ++b ) c |= ( ( cur[b] >> r ) & 1u ) << b;
+            const uint32_t Eq = s_eq[c * kDPThreads + threadIdx.x];
+            const uint32_t Xv = Eq | Mv;
+            const uint32_t s1 = ( Eq & Pv ) + Pv;
+            const uint32_t Xh = ( s1 ^ Pv ) | Eq;
             const uint32_t Ph = Mv | ~( Xh | Pv );
             const uint32_t Mhs = Pv & Xh & C.NGm1;
             const uint32_t mh = Pv & Xh & C.HB;
@@ -698,7 +710,13 @@ static void launch_struct_b ( const StructArgs & a, bool ed, dim3 grid, size_t s
     const bool block = ! getenv ( "MOTEX_STRUCT_NO_BLOCK" );
     if ( ed && ! getenv ( "MOTEX_STRUCT_NO_SWAR" ) && hswar_shape ( a, &C ) )
     {
-        if ( block ) k_dp_struct1_swar_blk<B><<<grid, kDPThreads, smem, st>>> ( a, C );
+        if ( block )
+        {
+            // + the per-thread Eq table of the block kernel
+            const size_t smem_t = smem + ( size_t ) ( 1 << B ) * kDPThreads * sizeof ( uint32_t );
+            cudaFuncSetAttribute ( k_dp_struct1_swar_blk<B>, cudaFuncAttributeMaxDynamicSharedMemorySize, ( int ) smem_t );
+            k_dp_struct1_swar_blk<B><<<grid, kDPThreads, smem_t, st>>> ( a, C );
+        }
         else k_dp_struct1_swar<B><<<grid, kDPThreads, smem, st>>> ( a, C );
     }
     else if ( ed )

@@ -146,12 +146,13 @@ __global__ void __launch_bounds__ ( kDPThreads ) k_dp_swar_ed ( const DPArgs a, 
 template <int B, int W, int UR>
 static void launch_fast_bwu ( const DPArgs & a, bool ed, dim3 grid, cudaStream_t st )
 {
+    const size_t smem = fast_smem_bytes ( B, W, ed );
     if ( ! ed )
         k_dp_fast<B, W, false, false, UR><<<grid, kDPThreads, 0, st>>> ( a );
     else if ( a.l <= 28 )
-        k_dp_fast<B, W, true, true, UR><<<grid, kDPThreads, 0, st>>> ( a );
+        k_dp_fast<B, W, true, true, UR><<<grid, kDPThreads, smem, st>>> ( a );
     else
-        k_dp_fast<B, W, true, false, UR><<<grid, kDPThreads, 0, st>>> ( a );
+        k_dp_fast<B, W, true, false, UR><<<grid, kDPThreads, smem, st>>> ( a );
 }
 
 template <int B, int W>

@@ -75,6 +75,16 @@ __device__ __forceinline__ void finish_chunk ( const DPArgs & a, const ChunkInfo
 
 using namespace dp_detail;
 
+/*
+ * Shared memory of the 1-lane body: none for Hamming; for edit distance with
+ * B <= 3 the per-thread match table Eq[code][register][thread] (Myers Peq of
+ * each of the thread's W factors against each symbol code).
+ */
+__host__ __device__ constexpr size_t fast_smem_bytes ( int B, int W, bool ed )
+{
+    return ( ed && B <= 3 ) ? ( size_t ) ( 1 << B ) * W * kDPThreads * sizeof ( uint32_t ) : 0;
+}
+
 template <int B, int W, bool ED, bool SCALED, int UR>
 __device__ __forceinline__ void dp_fast_body ( const DPArgs & a, uint32_t tile, uint32_t chunk )
 {
@@ -169,12 +179,20 @@ __device__ __forceinline__ void dp_fast_body ( const DPArgs & a, uint32_t tile, 
         uint32_t Pv[W], Mv[W], sc[W];
 #pragma unroll
         for ( int i = 0; i < W; ++i ) { Pv[i] = 0xffffffffu; Mv[i] = 0; sc[i] = sc0; }
-
-        auto step = [&] ( int i, const uint32_t ( &T )[B] ) {
-            uint32_t x = wp[i][0] ^ T[0];
+        constexpr bool TAB = B <= 3;
+        extern __shared__ uint32_t smem[];
+        uint32_t * s_eq = smem;                                  // [code][register][thread]
+        if constexpr ( TAB )
+            for ( int c = 0; c < ( 1 << B ); ++c )
 #pragma unroll
-            for ( int b = 1; b < B; ++b ) x |= wp[i][b] ^ T[b];
-            const uint32_t Eq = ~x;
+                for ( int i = 0; i < W; ++i )
+                {
+                    uint32_t x = 0;
+#pragma unroll
+                    for ( int b = 0; b < B; ++b ) x |= wp[i][b] ^ ( ( ( c >> b ) & 1 ) ? 0xffffffffu : 0u );
+                    s_eq[( c * W + i ) * kDPThreads + threadIdx.x] = ~x;
+                }
+        auto step_eq = [&] ( int i, const uint32_t Eq ) {
             const uint32_t Xv = Eq | Mv[i];
             const uint32_t Xh = ( ( ( Eq & Pv[i] ) + Pv[i] ) ^ Pv[i] ) | Eq;
             uint32_t Ph = Mv[i] | ~( Xh | Pv[i] );
@@ -187,6 +205,19 @@ __device__ __forceinline__ void dp_fast_body ( const DPArgs & a, uint32_t tile, 
             Mh <<= 1;
             Pv[i] = Mh | ~( Xv | Ph );
             Mv[i] = Ph & Xv;
+        };
+        auto step = [&] ( int i, const uint32_t ( &T )[B] ) {
+            uint32_t x = wp[i][0] ^ T[0];
+#pragma unroll
+            for ( int b = 1; b < B; ++b ) x |= wp[i][b] ^ T[b];
+            step_eq ( i, ~x );
+        };
+        // table row of the symbol at bit r of the plane words
+        auto eq_row = [&] ( const uint32_t ( &pw )[B], int r ) {
+            uint32_t c = 0;
+#pragma unroll
+            for ( int b = 0; b < B; ++b ) c |= ( ( pw[b] >> r ) & 1u ) << b;
+            return s_eq + c * ( W * kDPThreads ) + threadIdx.x;
         };
 
         uint32_t cur[B];
@@ -207,14 +238,27 @@ __device__ __forceinline__ void dp_fast_body ( const DPArgs & a, uint32_t tile, 
 #pragma unroll
                     for ( int rr = 0; rr < UR; ++rr )
                     {
-                        uint32_t T[B];
-#pragma unroll
-                        for ( int b = 0; b < B; ++b ) T[b] = 0u - ( ( cg[b] >> rr ) & 1u );
-#pragma unroll
-                        for ( int i = 0; i < W; ++i )
+                        if constexpr ( TAB )
                         {
-                            step ( i, T );
-                            cnt[i] += sc[i] < thr;
+                            const uint32_t * row = eq_row ( cg, rr );
+#pragma unroll
+                            for ( int i = 0; i < W; ++i )
+                            {
+                                step_eq ( i, row[i * kDPThreads] );
+                                cnt[i] += sc[i] < thr;
+                            }
+                        }
+                        else
+                        {
+                            uint32_t T[B];
+#pragma unroll
+                            for ( int b = 0; b < B; ++b ) T[b] = 0u - ( ( cg[b] >> rr ) & 1u );
+#pragma unroll
+                            for ( int i = 0; i < W; ++i )
+                            {
+                                step ( i, T );
+                                cnt[i] += sc[i] < thr;
+                            }
                         }
                     }
                 }
@@ -223,15 +267,28 @@ __device__ __forceinline__ void dp_fast_body ( const DPArgs & a, uint32_t tile, 
             {
                 for ( int r = 0; r < 32; ++r )
                 {
-                    uint32_t T[B];
-#pragma unroll
-                    for ( int b = 0; b < B; ++b ) T[b] = 0u - ( ( cur[b] >> r ) & 1u );
                     const bool count_here = counting && ( ( vm >> r ) & 1u );
-#pragma unroll
-                    for ( int i = 0; i < W; ++i )
+                    if constexpr ( TAB )
                     {
-                        step ( i, T );
-                        if ( count_here ) cnt[i] += sc[i] < thr;
+                        const uint32_t * row = eq_row ( cur, r );
+#pragma unroll
+                        for ( int i = 0; i < W; ++i )
+                        {
+                            step_eq ( i, row[i * kDPThreads] );
+                            if ( count_here ) cnt[i] += sc[i] < thr;
+                        }
+                    }
+                    else
+                    {
+                        uint32_t T[B];
+#pragma unroll
+                        for ( int b = 0; b < B; ++b ) T[b] = 0u - ( ( cur[b] >> r ) & 1u );
+#pragma unroll
+                        for ( int i = 0; i < W; ++i )
+                        {
+                            step ( i, T );
+                            if ( count_here ) cnt[i] += sc[i] < thr;
+                        }
                     }
                     if ( ( em >> r ) & 1u )
                     {

@@ -50,13 +50,15 @@ bool launch_b ( const JobDesc * jobs, const WorkItem * items, uint32_t nitems, u
         }
         else if ( scaled )
         {
-            if ( occ ) { *occ = ctas_per_sm ( k_dp_fast_persist<B, W, true, true, 8>, 0 ); return true; }
-            k_dp_fast_persist<B, W, true, true, 8><<<grid, kDPThreads, 0, st>>> ( jobs, items, nitems, counter );
+            const size_t smem = fast_smem_bytes ( B, W, true );
+            if ( occ ) { *occ = ctas_per_sm ( k_dp_fast_persist<B, W, true, true, 8>, smem ); return true; }
+            k_dp_fast_persist<B, W, true, true, 8><<<grid, kDPThreads, smem, st>>> ( jobs, items, nitems, counter );
         }
         else
         {
-            if ( occ ) { *occ = ctas_per_sm ( k_dp_fast_persist<B, W, true, false, 8>, 0 ); return true; }
-            k_dp_fast_persist<B, W, true, false, 8><<<grid, kDPThreads, 0, st>>> ( jobs, items, nitems, counter );
+            const size_t smem = fast_smem_bytes ( B, W, true );
+            if ( occ ) { *occ = ctas_per_sm ( k_dp_fast_persist<B, W, true, false, 8>, smem ); return true; }
+            k_dp_fast_persist<B, W, true, false, 8><<<grid, kDPThreads, smem, st>>> ( jobs, items, nitems, counter );
         }
         return true;
     }

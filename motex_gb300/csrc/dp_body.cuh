@@ -339,15 +339,22 @@ __device__ __forceinline__ bool next_item ( const WorkItem * items, uint32_t nit
 
 /*
  * Shared memory of the SWAR body: hit counters [field][thread] (count in the
- * current text, texts seen, occurrences) and, for B <= 3, the per-thread
- * match table Eq[code][register][thread]: the Myers Eq vector of each of the
- * thread's W registers against each symbol code, so a step reads Eq with one
- * shared-memory load (LSU pipe) instead of forming it from the bit planes.
+ * current text, texts seen, occurrences) and the per-thread match table
+ * Eq[code][register][thread]: the Myers Eq vector of each of the thread's W
+ * registers against each symbol code, so a step reads Eq with shared-memory
+ * loads (LSU pipe) instead of forming it from the bit planes.  B <= 3: one
+ * row per code; B = 4, 5: the low-three-bit and high-bit tables below.
  */
 __host__ __device__ constexpr bool swar_table ( int B ) { return B <= 3; }
+// B = 4, 5: Eq is a conjunction over the planes, so it splits into a table of
+// the low three code bits and one of the high bits: Eq = lo[c & 7] & hi[c >> 3]
+__host__ __device__ constexpr size_t swar_table_words ( int B )
+{
+    return swar_table ( B ) ? ( size_t ) ( 1 << B ) : ( size_t ) ( 8 + ( 1 << ( B - 3 ) ) );
+}
 __host__ __device__ constexpr size_t swar_smem_bytes ( int B, int NL, int W )
 {
-    return ( ( size_t ) 3 * W * NL + ( swar_table ( B ) ? ( size_t ) ( 1 << B ) * W : 0 ) ) * kDPThreads * sizeof ( uint32_t );
+    return ( ( size_t ) 3 * W * NL + swar_table_words ( B ) * W ) * kDPThreads * sizeof ( uint32_t );
 }
 
 template <int B, int NL, int W, int UR>
@@ -385,6 +392,28 @@ __device__ __forceinline__ void dp_swar_body ( const DPArgs & a, const SwarConst
     for ( int i = 0; i < W; ++i ) { Pv[i] = C.NG; Mv[i] = 0; sc[i] = C.SC0; cnt[i] = 0; }
     constexpr bool TAB = swar_table ( B );
     uint32_t * s_eq = smem + 3 * NF * kDPThreads;            // [code][register][thread]
+    uint32_t * s_hi = s_eq + 8 * W * kDPThreads;             // B = 4, 5: [high bits][register][thread]
+    if constexpr ( ! TAB )
+    {
+        for ( int c = 0; c < 8; ++c )
+#pragma unroll
+            for ( int i = 0; i < W; ++i )
+            {
+                uint32_t x = 0;
+#pragma unroll
+                for ( int b = 0; b < 3; ++b ) x |= wp[i][b] ^ ( ( ( c >> b ) & 1 ) ? C.NG : 0u );
+                s_eq[( c * W + i ) * kDPThreads + tid] = ~x;
+            }
+        for ( int c = 0; c < ( 1 << ( B - 3 ) ); ++c )
+#pragma unroll
+            for ( int i = 0; i < W; ++i )
+            {
+                uint32_t x = 0;
+#pragma unroll
+                for ( int b = 3; b < B; ++b ) x |= wp[i][b] ^ ( ( ( c >> ( b - 3 ) ) & 1 ) ? C.NG : 0u );
+                s_hi[( c * W + i ) * kDPThreads + tid] = ~x;
+            }
+    }
     if constexpr ( TAB )
     {
         // text bits are cleared at the guards, so Eq is 1 there (lanes stay apart)
@@ -484,6 +513,18 @@ __device__ __forceinline__ void dp_swar_body ( const DPArgs & a, const SwarConst
                             count ( i );
                         }
                     }
+                    else if constexpr ( true )
+                    {
+                        const uint32_t c = code_at ( cg, rr );
+                        const uint32_t * lo = s_eq + ( c & 7u ) * ( W * kDPThreads ) + tid;
+                        const uint32_t * hi = s_hi + ( c >> 3 ) * ( W * kDPThreads ) + tid;
+#pragma unroll
+                        for ( int i = 0; i < W; ++i )
+                        {
+                            step_eq ( i, lo[i * kDPThreads] & hi[i * kDPThreads] );
+                            count ( i );
+                        }
+                    }
                     else
                     {
                         uint32_t T[B];
@@ -511,6 +552,18 @@ __device__ __forceinline__ void dp_swar_body ( const DPArgs & a, const SwarConst
                     for ( int i = 0; i < W; ++i )
                     {
                         step_eq ( i, row[i * kDPThreads] );
+                        if ( count_here ) count ( i );
+                    }
+                }
+                else if constexpr ( true )
+                {
+                    const uint32_t c = code_at ( cur, r );
+                    const uint32_t * lo = s_eq + ( c & 7u ) * ( W * kDPThreads ) + tid;
+                    const uint32_t * hi = s_hi + ( c >> 3 ) * ( W * kDPThreads ) + tid;
+#pragma unroll
+                    for ( int i = 0; i < W; ++i )
+                    {
+                        step_eq ( i, lo[i * kDPThreads] & hi[i * kDPThreads] );
                         if ( count_here ) count ( i );
                     }
                 }

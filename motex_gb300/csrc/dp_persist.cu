@@ -65,11 +65,12 @@ bool launch_b ( const JobDesc * jobs, const WorkItem * items, uint32_t nitems, u
 #define MTX_SWAR_P( NLV )                                                                                   \
     case NLV:                                                                                               \
     {                                                                                                       \
-        const size_t smem = swar_smem_bytes ( B, NLV, W );                                                  \
-        if ( occ ) { *occ = ctas_per_sm ( k_dp_swar_persist<B, NLV, W, 8>, smem ); return true; }            \
-        cudaFuncSetAttribute ( k_dp_swar_persist<B, NLV, W, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize,   \
+        constexpr int WS = swar_default_w ( B );                                                            \
+        const size_t smem = swar_smem_bytes ( B, NLV, WS );                                                 \
+        if ( occ ) { *occ = ctas_per_sm ( k_dp_swar_persist<B, NLV, WS, 8>, smem ); return true; }           \
+        cudaFuncSetAttribute ( k_dp_swar_persist<B, NLV, WS, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize,  \
                                ( int ) smem );                                                              \
-        k_dp_swar_persist<B, NLV, W, 8><<<grid, kDPThreads, smem, st>>> ( jobs, items, nitems, counter );     \
+        k_dp_swar_persist<B, NLV, WS, 8><<<grid, kDPThreads, smem, st>>> ( jobs, items, nitems, counter );    \
         return true;                                                                                        \
     }
     switch ( NL )

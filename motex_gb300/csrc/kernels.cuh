@@ -159,6 +159,11 @@ struct SwarConst
     uint32_t FM;     // field mask (S bits)
 };
 SwarConst swar_const ( uint32_t l, uint32_t e, int NL );
+// Register words per thread of the packed kernels when the shape is not tuned
+// (batched jobs, persistent launches, the default of an untuned job): with
+// B = 4, 5 the split Eq table leaves room for enough CTAs per SM only at
+// W = 4 (measured on config 3: W = 4 runs 352 ms, W = 8 393 ms).
+__host__ __device__ constexpr int swar_default_w ( int B ) { return B >= 4 ? 4 : 8; }
 
 // One job of a batched launch and one unit of its work.
 struct JobDesc

@@ -386,6 +386,7 @@ DPTune choose_tune ( Job * j, uint32_t U, bool ed, bool generic )
     t.NL = ed ? swar_lanes ( j->prm.l ) : 1;
     const uint32_t groups = ( U + t.NL - 1 ) / t.NL;
     t.W = groups >= ( uint32_t ) j->ctx->num_sms * kDPThreads * 8 ? 8 : 4;
+    if ( t.NL > 1 ) t.W = std::min ( t.W, swar_default_w ( j->B ) );
     t.UR = ed ? 8 : 4;             // measured on GB300: Hamming prefers the shorter body
     if ( const char * e = getenv ( "MOTEX_DP_SWAR" ) )
         if ( atoi ( e ) == 0 ) t.NL = 1;
@@ -1387,10 +1388,10 @@ int batch_dp ( motex_ctx * c, std::vector<Job *> & jobs, float * dp_ms )
         }
         const bool ed = j->prm.d == 1;
         Class k { j->B < 2 ? 2 : j->B, ed, ed && j->prm.l <= 28 && j->tune.NL == 1, j->tune.NL };
-        // the persistent kernels hold 8 register words per thread
-        j->tune.W = 8;
+        // register words per thread of the persistent kernels
+        j->tune.W = j->tune.NL > 1 ? swar_default_w ( k.B ) : 8;
         const uint32_t groups = ( j->U + j->tune.NL - 1 ) / j->tune.NL;
-        j->ntiles = ( groups + kDPThreads * 8 - 1 ) / ( kDPThreads * 8 );
+        j->ntiles = ( groups + kDPThreads * j->tune.W - 1 ) / ( kDPThreads * j->tune.W );
         classes[k].push_back ( j );
     }
     size_t njobs = 0, nitems = 0;

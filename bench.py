@@ -89,7 +89,7 @@ def cpu_binary():
     return PORT, "port"
 
 
-def cpu_run(binary, wl, seqs, threads):
+def cpu_run(binary, wl, seqs, threads, timeout=600):
     """Run the CPU implementation on seqs; returns (cells, secs) of its own all-pairs timer."""
     with tempfile.TemporaryDirectory() as tmp:
         fa, out = os.path.join(tmp, "in.fa"), os.path.join(tmp, "out.motex")
@@ -99,7 +99,7 @@ def cpu_run(binary, wl, seqs, threads):
             bx = os.path.join(tmp, "in.boxes")
             W.write_boxes(bx, wl.boxes)
             args[args.index("-s") + 1] = bx
-        p = subprocess.run([binary] + args, capture_output=True, text=True)
+        p = subprocess.run([binary] + args, capture_output=True, text=True, timeout=timeout)
         if p.returncode != 0:
             raise RuntimeError(f"{binary} failed: {p.stderr[-500:]}")
         m = re.search(r"# Run on \d+ proc\(s\) in ([0-9.]+) secs", open(out).read())
@@ -109,18 +109,35 @@ def cpu_run(binary, wl, seqs, threads):
     return searched * searched * (len(wl.boxes) + 1), secs
 
 
-def cpu_sample(binary, wl, threads, target_s=CPU_SAMPLE_SECONDS):
-    """Largest prefix of the workload's sequences that runs in about target_s."""
-    n = max(2, min(len(wl.seqs), 16))
-    while True:
-        cells, secs = cpu_run(binary, wl, wl.seqs[:n], threads)
-        if n >= len(wl.seqs) or secs >= target_s / 4:
+def take_symbols(seqs, total):
+    """The first `total` symbols of a workload: its sequences in order, the last one cut."""
+    out, left = [], total
+    for s in seqs:
+        if left <= 0:
             break
-        n = min(len(wl.seqs), max(n + 1, int(n * 2)))
-    # cost grows ~ quadratically in the number of sequences
-    scale = (target_s / max(secs, 1e-3)) ** 0.5
-    n2 = max(2, min(len(wl.seqs), int(n * scale)))
-    return wl.seqs[:n2]
+        out.append(s[:left])
+        left -= len(out[-1])
+    return out
+
+
+def cpu_sample(binary, wl, threads, target_s=CPU_SAMPLE_SECONDS):
+    """(sequences, description): the largest prefix of the workload, counted in
+    symbols, whose CPU run takes about target_s.  The cost grows with the
+    square of the symbols, so the probe starts at 20k symbols and doubles
+    until a run takes a quarter of the target."""
+    total = sum(map(len, wl.seqs))
+    t = min(total, 20000)
+    while True:
+        cells, secs = cpu_run(binary, wl, take_symbols(wl.seqs, t), threads, timeout=max(120, 20 * target_s))
+        if t >= total or secs >= target_s / 4:
+            break
+        t = min(total, t * 2)
+    t2 = max(1, min(total, int(t * (target_s / max(secs, 1e-3)) ** 0.5)))
+    sample = take_symbols(wl.seqs, t2)
+    cut = len(sample[-1]) < len(wl.seqs[len(sample) - 1])
+    desc = (f"first {t2} of {total} symbols ({len(sample)} of {len(wl.seqs)} sequences"
+            + (f", the last cut to {len(sample[-1])}" if cut else "") + ")")
+    return sample, desc
 
 
 # ---------------------------------------------------------------- clocks
@@ -437,7 +454,7 @@ def run_reference(args):
     wl = WORKLOADS[args.workload](args.scale)
     binary, kind = cpu_binary()
     threads = os.cpu_count() or 1
-    sample = cpu_sample(binary, wl, threads, target_s=8.0)
+    sample, sample_desc = cpu_sample(binary, wl, threads, target_s=8.0)
     for _ in range(args.warmup):
         cpu_run(binary, wl, sample, threads)
     cells_t, secs_t = 0, 0.0
@@ -446,7 +463,7 @@ def run_reference(args):
         cells_t += c
         secs_t += s
     val = cells_t / secs_t / 1e9
-    desc = f"first {len(sample)} of {len(wl.seqs)} sequences ({sum(map(len, sample))} symbols)"
+    desc = sample_desc
     return {
         "impl": "reference", "metric": "GCUPS (reference DP cell updates per second), whole-set word-based motif extraction",
         "value": round(val, 3), "unit": "GCUPS", "n_gpus": 0, "steps": args.steps, "warmup": args.warmup,
@@ -492,11 +509,10 @@ def main():
         if not args.no_cpu_baseline:
             binary, kind = cpu_binary()
             threads = os.cpu_count() or 1
-            sample = cpu_sample(binary, wl, threads)
+            sample, desc = cpu_sample(binary, wl, threads)
             cells, secs = cpu_run(binary, wl, sample, threads)
             out["cpu_baseline"] = {"value": round(cells / secs / 1e9, 3), "unit": "GCUPS", "cores": threads,
-                                   "kind": kind,
-                                   "sample": f"first {len(sample)} of {len(wl.seqs)} sequences, {secs:.1f} s"}
+                                   "kind": kind, "sample": f"{desc}, {secs:.1f} s"}
         print(json.dumps(out), flush=True)
     if world > 1:
         import torch.distributed as dist

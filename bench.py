@@ -237,12 +237,18 @@ def aggregate_replicas(step_s, e2e_s, cells, world):
 
 
 def dp_kernel_name(wl):
+    """The engine's default DP kernel for the workload (bit planes B from the
+    symbols present; the autotuner may pick another shape of the same kernel)."""
     if wl.boxes:
         return "k_dp_struct1"
     if wl.k > 32:
         return "k_dp_generic"
+    sigma = len(set("".join(wl.seqs)))
+    B = max(2, (sigma - 1).bit_length())
     if wl.d == 1 and 4 <= wl.k <= 15:
         return f"k_dp_swar_ed (NL={min(4, 33 // (wl.k + 1))})"
+    if wl.d == 0 and B >= 3 and 6 <= wl.k <= 16:
+        return f"k_dp_hswar (NL={32 // wl.k})"
     return "k_dp_fast"
 
 

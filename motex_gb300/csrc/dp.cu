@@ -141,6 +141,12 @@ __global__ void __launch_bounds__ ( kDPThreads ) k_dp_swar_ed ( const DPArgs a, 
     dp_swar_body<B, NL, W, UR> ( a, C, blockIdx.x, blockIdx.y );
 }
 
+template <int B, int NL, int W, int UR>
+__global__ void __launch_bounds__ ( kDPThreads ) k_dp_hswar ( const DPArgs a, const SwarConst C )
+{
+    dp_hswar_body<B, NL, W, UR> ( a, C, blockIdx.x, blockIdx.y );
+}
+
 // ------------------------------------------------------------------ launchers
 
 template <int B, int W, int UR>
@@ -270,6 +276,61 @@ bool launch_dp_swar_ed ( const DPArgs & a, int B, int NL, int W, int UR, dim3 gr
         case 3: return launch_swar_b<3> ( a, C, NL, W, UR, grid, st );
         case 4: return launch_swar_b<4> ( a, C, NL, W, UR, grid, st );
         case 5: return launch_swar_b<5> ( a, C, NL, W, UR, grid, st );
+        default: return false;
+    }
+}
+
+int hswar_lanes ( uint32_t l ) { return ( l >= 6 && l <= 16 ) ? ( int ) ( 32 / l ) : 1; }
+
+SwarConst hswar_const ( uint32_t l, int NL )
+{
+    SwarConst C {};
+    C.S = l;
+    C.FM = ( 1u << l ) - 1u;
+    for ( int j = 0; j < NL; ++j ) C.REP |= 1u << ( j * l );
+    return C;
+}
+
+template <int B, int NL, int W>
+static bool launch_hswar_bnw ( const DPArgs & a, const SwarConst & C, dim3 grid, cudaStream_t st )
+{
+    const size_t smem = hswar_smem_bytes ( NL, W );
+    cudaFuncSetAttribute ( k_dp_hswar<B, NL, W, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, ( int ) smem );
+    k_dp_hswar<B, NL, W, 4><<<grid, kDPThreads, smem, st>>> ( a, C );
+    return true;
+}
+
+template <int B, int NL>
+static bool launch_hswar_bn ( const DPArgs & a, const SwarConst & C, int W, dim3 grid, cudaStream_t st )
+{
+    if ( W == 8 ) return launch_hswar_bnw<B, NL, 8> ( a, C, grid, st );
+    if ( W == 4 ) return launch_hswar_bnw<B, NL, 4> ( a, C, grid, st );
+    return false;
+}
+
+template <int B>
+static bool launch_hswar_b ( const DPArgs & a, const SwarConst & C, int NL, int W, dim3 grid, cudaStream_t st )
+{
+    switch ( NL )
+    {
+        case 2: return launch_hswar_bn<B, 2> ( a, C, W, grid, st );
+        case 3: return launch_hswar_bn<B, 3> ( a, C, W, grid, st );
+        case 4: return launch_hswar_bn<B, 4> ( a, C, W, grid, st );
+        case 5: return launch_hswar_bn<B, 5> ( a, C, W, grid, st );
+        default: return false;
+    }
+}
+
+// Packed Hamming kernels (unroll 4, the Hamming optimum) for 3-5 bit planes.
+bool launch_dp_hswar ( const DPArgs & a, int B, int NL, int W, int, dim3 grid, cudaStream_t st )
+{
+    if ( NL < 2 || NL != hswar_lanes ( a.l ) ) return false;
+    const SwarConst C = hswar_const ( a.l, NL );
+    switch ( B )
+    {
+        case 3: return launch_hswar_b<3> ( a, C, NL, W, grid, st );
+        case 4: return launch_hswar_b<4> ( a, C, NL, W, grid, st );
+        case 5: return launch_hswar_b<5> ( a, C, NL, W, grid, st );
         default: return false;
     }
 }

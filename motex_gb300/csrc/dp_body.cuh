@@ -612,4 +612,159 @@ __device__ __forceinline__ void dp_swar_body ( const DPArgs & a, const SwarConst
     }
 }
 
+/*
+ * Hamming, NL factors of l bits per register (lane j at bits [j*l, j*l+l),
+ * symbol q of the factor at bit j*l+q; no guard bits, XOR and OR do not
+ * carry).  Per text position the l-symbol window of each plane is shifted
+ * down to bit 0 and replicated into every lane by one multiply with
+ * REP = sum 2^(j*l) (the lanes do not overlap, so the product does not
+ * carry); then each register costs B XOR/ORs for its NL factors, and each
+ * lane a masked popc.  Hit counts live in l-bit register fields (l >= 6
+ * holds a 32-position block), drained to shared memory per block like the
+ * edit-distance SWAR body.
+ */
+template <int B, int NL, int W, int UR>
+__device__ __forceinline__ void dp_hswar_body ( const DPArgs & a, const SwarConst & C, uint32_t tile, uint32_t chunk )
+{
+    extern __shared__ uint32_t smem[];
+    constexpr int NF = W * NL;
+    uint32_t * s_cnt = smem;
+    uint32_t * s_u = smem + NF * kDPThreads;
+    uint32_t * s_v = smem + 2 * NF * kDPThreads;
+    const int tid = threadIdx.x;
+    for ( int f = 0; f < NF; ++f ) s_cnt[f * kDPThreads + tid] = s_u[f * kDPThreads + tid] = s_v[f * kDPThreads + tid] = 0;
+
+    const uint32_t gbase = tile * ( kDPThreads * W ) + tid;
+    const uint32_t l = a.l, down = 32 - l, e = a.e;
+    uint32_t fp[W][B];
+#pragma unroll
+    for ( int i = 0; i < W; ++i )
+    {
+#pragma unroll
+        for ( int b = 0; b < B; ++b ) fp[i][b] = 0;
+        const uint32_t g = gbase + i * kDPThreads;
+#pragma unroll
+        for ( int j = 0; j < NL; ++j )
+        {
+            const uint32_t w = g * NL + j;
+            if ( w < a.U )
+#pragma unroll
+                for ( int b = 0; b < B; ++b ) fp[i][b] |= ( __ldg ( a.wplanes32 + ( size_t ) b * a.U + w ) >> down ) << ( j * C.S );
+        }
+    }
+    uint32_t cnt[W];
+#pragma unroll
+    for ( int i = 0; i < W; ++i ) cnt[i] = 0;
+
+    const ChunkInfo ch = a.chunks[chunk];
+    int cur_split = ch.first_split;
+    const uint32_t * __restrict__ planes = a.text.planes;
+    const uint32_t stride = a.text.plane_stride;
+
+    auto count = [&] ( int i, const uint32_t ( &Y )[B] ) {
+        uint32_t x = fp[i][0] ^ Y[0];
+#pragma unroll
+        for ( int b = 1; b < B; ++b ) x |= fp[i][b] ^ Y[b];
+#pragma unroll
+        for ( int j = 0; j < NL; ++j )
+            if ( __popc ( x & ( C.FM << ( j * C.S ) ) ) <= e ) cnt[i] += 1u << ( j * C.S );
+    };
+    auto window = [&] ( const uint32_t ( &prev )[B], const uint32_t ( &cur )[B], int r, uint32_t ( &Y )[B] ) {
+#pragma unroll
+        for ( int b = 0; b < B; ++b ) Y[b] = ( __funnelshift_rc ( prev[b], cur[b], r + 1 ) >> down ) * C.REP;
+    };
+    auto drain = [&] () {
+#pragma unroll
+        for ( int i = 0; i < W; ++i )
+        {
+#pragma unroll
+            for ( int j = 0; j < NL; ++j ) s_cnt[( i * NL + j ) * kDPThreads + tid] += ( cnt[i] >> ( j * C.S ) ) & C.FM;
+            cnt[i] = 0;
+        }
+    };
+    auto end_sequence = [&] () {
+        for ( int f = 0; f < NF; ++f )
+        {
+            const uint32_t c = s_cnt[f * kDPThreads + tid];
+            if ( ! c ) continue;
+            if ( cur_split < 0 ) s_u[f * kDPThreads + tid] += 1;
+            else
+            {
+                const uint32_t w = ( gbase + ( f / NL ) * kDPThreads ) * NL + ( f % NL );
+                if ( w < a.U ) a.split_flags[( size_t ) cur_split * a.U + w] = 1;
+            }
+            s_v[f * kDPThreads + tid] += c;
+            s_cnt[f * kDPThreads + tid] = 0;
+        }
+    };
+
+    uint32_t prev[B];
+#pragma unroll
+    for ( int b = 0; b < B; ++b ) prev[b] = __ldg ( planes + ( size_t ) b * stride + ch.begin );
+    for ( uint32_t k = ch.begin; k < ch.end; ++k )
+    {
+        uint32_t cur[B];
+#pragma unroll
+        for ( int b = 0; b < B; ++b ) cur[b] = __ldg ( planes + ( size_t ) b * stride + k + 1 );
+        const uint32_t vm = __ldg ( a.text.vmask + k ), em = __ldg ( a.text.emask + k );
+        if ( vm == 0xffffffffu && em == 0u )
+        {
+#pragma unroll 1
+            for ( int g = 0; g < 32; g += UR )
+            {
+#pragma unroll
+                for ( int rr = 0; rr < UR; ++rr )
+                {
+                    uint32_t Y[B];
+                    window ( prev, cur, g + rr, Y );
+#pragma unroll
+                    for ( int i = 0; i < W; ++i ) count ( i, Y );
+                }
+            }
+        }
+        else
+        {
+            for ( int r = 0; r < 32; ++r )
+            {
+                if ( ( vm >> r ) & 1u )
+                {
+                    uint32_t Y[B];
+                    window ( prev, cur, r, Y );
+#pragma unroll
+                    for ( int i = 0; i < W; ++i ) count ( i, Y );
+                }
+                if ( ( em >> r ) & 1u )
+                {
+                    drain ();
+                    end_sequence ();
+                    cur_split = -1;
+                }
+            }
+        }
+        drain ();
+#pragma unroll
+        for ( int b = 0; b < B; ++b ) prev[b] = cur[b];
+    }
+    for ( int f = 0; f < NF; ++f )
+    {
+        const uint32_t w = ( gbase + ( f / NL ) * kDPThreads ) * NL + ( f % NL );
+        if ( w >= a.U ) continue;
+        const uint32_t c = s_cnt[f * kDPThreads + tid];
+        uint32_t u = s_u[f * kDPThreads + tid];
+        if ( c )
+        {
+            if ( ch.last_split >= 0 ) a.split_flags[( size_t ) ch.last_split * a.U + w] = 1;
+            else u += 1;
+        }
+        const uint32_t v = s_v[f * kDPThreads + tid] + c;
+        if ( u ) atomicAdd ( a.u_acc + w, u );
+        if ( v ) atomicAdd ( a.v_acc + w, v );
+    }
+}
+
+__host__ __device__ constexpr size_t hswar_smem_bytes ( int NL, int W )
+{
+    return ( size_t ) 3 * W * NL * kDPThreads * sizeof ( uint32_t );
+}
+
 } // namespace mtx

@@ -16,6 +16,15 @@ __global__ void __launch_bounds__ ( kDPThreads ) k_dp_fast_persist ( const JobDe
 }
 
 template <int B, int NL, int W, int UR>
+__global__ void __launch_bounds__ ( kDPThreads ) k_dp_hswar_persist ( const JobDesc * jobs, const WorkItem * items,
+                                                                      uint32_t nitems, uint32_t * counter )
+{
+    WorkItem w;
+    while ( next_item ( items, nitems, counter, w ) )
+        dp_hswar_body<B, NL, W, UR> ( jobs[w.job].a, jobs[w.job].C, w.tile, w.chunk );
+}
+
+template <int B, int NL, int W, int UR>
 __global__ void __launch_bounds__ ( kDPThreads ) k_dp_swar_persist ( const JobDesc * jobs, const WorkItem * items,
                                                                      uint32_t nitems, uint32_t * counter )
 {
@@ -61,6 +70,33 @@ bool launch_b ( const JobDesc * jobs, const WorkItem * items, uint32_t nitems, u
             k_dp_fast_persist<B, W, true, false, 8><<<grid, kDPThreads, smem, st>>> ( jobs, items, nitems, counter );
         }
         return true;
+    }
+    if ( ! ed )
+    {
+        // packed Hamming (3-5 bit planes), 8 register words per thread
+        if constexpr ( B >= 3 )
+        {
+#define MTX_HSWAR_P( NLV )                                                                                  \
+    case NLV:                                                                                               \
+    {                                                                                                       \
+        const size_t smem = hswar_smem_bytes ( NLV, 8 );                                                    \
+        if ( occ ) { *occ = ctas_per_sm ( k_dp_hswar_persist<B, NLV, 8, 4>, smem ); return true; }           \
+        cudaFuncSetAttribute ( k_dp_hswar_persist<B, NLV, 8, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize,  \
+                               ( int ) smem );                                                              \
+        k_dp_hswar_persist<B, NLV, 8, 4><<<grid, kDPThreads, smem, st>>> ( jobs, items, nitems, counter );    \
+        return true;                                                                                        \
+    }
+            switch ( NL )
+            {
+                MTX_HSWAR_P ( 2 )
+                MTX_HSWAR_P ( 3 )
+                MTX_HSWAR_P ( 4 )
+                MTX_HSWAR_P ( 5 )
+                default: return false;
+            }
+#undef MTX_HSWAR_P
+        }
+        return false;
     }
 #define MTX_SWAR_P( NLV )                                                                                   \
     case NLV:                                                                                               \

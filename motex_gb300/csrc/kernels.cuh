@@ -157,8 +157,15 @@ struct SwarConst
     uint32_t SC0;    // per field score l
     uint32_t S;      // lane stride
     uint32_t FM;     // field mask (S bits)
+    uint32_t REP;    // Hamming lanes: sum of 2^(j*l), replicates an l-bit window into every lane
 };
 SwarConst swar_const ( uint32_t l, uint32_t e, int NL );
+// Hamming with NL = hswar_lanes(l) >= 2 factors of l bits per register
+// (6 <= l <= 16, no guard bits: XOR and OR do not carry); kernels exist for
+// B = 3..5 (the protein case; DNA gains nothing).
+int hswar_lanes ( uint32_t l );
+SwarConst hswar_const ( uint32_t l, int NL );
+bool launch_dp_hswar ( const DPArgs & a, int B, int NL, int W, int UR, dim3 grid, cudaStream_t st );
 // Register words per thread of the packed kernels when the shape is not tuned
 // (batched jobs, persistent launches, the default of an untuned job): with
 // B = 4, 5 the split Eq table leaves room for enough CTAs per SM only at

@@ -383,7 +383,7 @@ DPTune choose_tune ( Job * j, uint32_t U, bool ed, bool generic )
 {
     DPTune t;
     if ( generic ) { t.W = 1; t.NL = 1; t.UR = 32; return t; }
-    t.NL = ed ? swar_lanes ( j->prm.l ) : 1;
+    t.NL = ed ? swar_lanes ( j->prm.l ) : ( j->B >= 3 ? hswar_lanes ( j->prm.l ) : 1 );
     const uint32_t groups = ( U + t.NL - 1 ) / t.NL;
     t.W = groups >= ( uint32_t ) j->ctx->num_sms * kDPThreads * 8 ? 8 : 4;
     if ( t.NL > 1 ) t.W = std::min ( t.W, swar_default_w ( j->B ) );
@@ -468,8 +468,10 @@ bool tune_lookup ( const TuneKey & k, DPTune * t )
 bool launch_shape ( Job * j, const DPArgs & da, const DPTune & t, dim3 grid )
 {
     const bool ed = j->prm.d == 1;
-    return t.NL > 1 ? launch_dp_swar_ed ( da, j->B, t.NL, t.W, t.UR, grid, j->ctx->st )
-                    : launch_dp_fast ( da, j->B, t.W, t.UR, ed, grid, j->ctx->st );
+    if ( t.NL > 1 )
+        return ed ? launch_dp_swar_ed ( da, j->B, t.NL, t.W, t.UR, grid, j->ctx->st )
+                  : launch_dp_hswar ( da, j->B, t.NL, t.W, t.UR, grid, j->ctx->st );
+    return launch_dp_fast ( da, j->B, t.W, t.UR, ed, grid, j->ctx->st );
 }
 
 int autotune ( Job * j, DPTune * best )
@@ -477,12 +479,13 @@ int autotune ( Job * j, DPTune * best )
     const bool ed = j->prm.d == 1;
     const TuneKey key { j->B, j->prm.l, j->prm.e, j->prm.d };
     std::vector<DPTune> cands;
-    for ( int NL : { swar_lanes ( j->prm.l ), 1 } )
+    const int packed = ed ? swar_lanes ( j->prm.l ) : ( j->B >= 3 ? hswar_lanes ( j->prm.l ) : 1 );
+    for ( int NL : { packed, 1 } )
     {
-        if ( ! ed && NL > 1 ) continue;
         for ( int W : { 4, 8 } )
             for ( int UR : { 4, 8 } )
-                cands.push_back ( DPTune { W, NL, UR } );
+                if ( ed || NL == 1 || UR == 4 )              // packed Hamming exists with unroll 4 only
+                    cands.push_back ( DPTune { W, NL, UR } );
         if ( NL == 1 ) break;
     }
     // probe chunks: consecutive 512-block ranges from the start of the text, no splits
@@ -998,7 +1001,8 @@ int stage_dp ( Job * j )
     {
         const dim3 grid ( j->ntiles, ( unsigned ) j->chunks.size () );
         ok = j->generic        ? launch_dp_generic ( j->da, j->B, j->nw64, ed, grid, st )
-             : j->tune.NL > 1  ? launch_dp_swar_ed ( j->da, j->B, j->tune.NL, j->tune.W, j->tune.UR, grid, st )
+             : j->tune.NL > 1  ? ( ed ? launch_dp_swar_ed ( j->da, j->B, j->tune.NL, j->tune.W, j->tune.UR, grid, st )
+                                        : launch_dp_hswar ( j->da, j->B, j->tune.NL, j->tune.W, j->tune.UR, grid, st ) )
                                : launch_dp_fast ( j->da, j->B, j->tune.W, j->tune.UR, ed, grid, st );
     }
     if ( ! ok ) return fail ( MOTEX_EUNSUPPORTED, "no DP kernel for l=%u B=%d", j->prm.l, j->B );
@@ -1389,7 +1393,7 @@ int batch_dp ( motex_ctx * c, std::vector<Job *> & jobs, float * dp_ms )
         const bool ed = j->prm.d == 1;
         Class k { j->B < 2 ? 2 : j->B, ed, ed && j->prm.l <= 28 && j->tune.NL == 1, j->tune.NL };
         // register words per thread of the persistent kernels
-        j->tune.W = j->tune.NL > 1 ? swar_default_w ( k.B ) : 8;
+        j->tune.W = ( j->tune.NL > 1 && ed ) ? swar_default_w ( k.B ) : 8;
         const uint32_t groups = ( j->U + j->tune.NL - 1 ) / j->tune.NL;
         j->ntiles = ( groups + kDPThreads * j->tune.W - 1 ) / ( kDPThreads * j->tune.W );
         classes[k].push_back ( j );
@@ -1423,7 +1427,9 @@ int batch_dp ( motex_ctx * c, std::vector<Job *> & jobs, float * dp_ms )
             for ( Job * j : kv.second )
             {
                 hj[jat].a = j->da;
-                hj[jat].C = j->tune.NL > 1 ? swar_const ( j->prm.l, j->prm.e, j->tune.NL ) : SwarConst {};
+                hj[jat].C = j->tune.NL <= 1 ? SwarConst {}
+                            : ( j->prm.d == 1 ? swar_const ( j->prm.l, j->prm.e, j->tune.NL )
+                                              : hswar_const ( j->prm.l, j->tune.NL ) );
                 const uint64_t words = ( uint64_t ) kDPThreads * j->tune.W * j->tune.NL;
                 for ( uint32_t ch = 0; ch < j->chunks.size (); ++ch )
                 {

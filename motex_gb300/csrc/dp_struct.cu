@@ -217,7 +217,7 @@ __global__ void __launch_bounds__ ( kDPThreads ) k_dp_struct1 ( const StructArgs
  * per-structure counts are those of k_dp_struct1; a sequence end flushes
  * and clears the history up to it.
  */
-template <int B>
+template <int B, bool PK>
 __global__ void __launch_bounds__ ( kDPThreads ) k_dp_struct1_hd ( const StructArgs a )
 {
     extern __shared__ uint32_t smem[];
@@ -261,6 +261,22 @@ __global__ void __launch_bounds__ ( kDPThreads ) k_dp_struct1_hd ( const StructA
     const uint32_t top0 = l0 >= 32 ? 0xffffffffu : ~( ( 1u << ( 32 - l0 ) ) - 1u );
     const uint32_t top1 = l1 >= 32 ? 0xffffffffu : ~( ( 1u << ( 32 - l1 ) ) - 1u );
     const uint32_t full = 0xffffffffu;
+    // PK: the three rows as lanes of L = max(l0, l1) <= 10 bits of one register
+    // (box 0, row r0, row r1), each factor in the top of its lane; the window's
+    // newest L symbols are replicated into the lanes by a multiply
+    const uint32_t L = l0 > l1 ? l0 : l1;
+    const uint32_t rep3 = 1u | ( 1u << L ) | ( 1u << ( 2 * L ) );
+    const uint32_t mA = ( ( 1u << l0 ) - 1u ) << ( L - l0 );
+    const uint32_t mB = ( ( 1u << l1 ) - 1u ) << ( 2 * L - l1 );
+    const uint32_t mC = ( ( 1u << l1 ) - 1u ) << ( 3 * L - l1 );
+    uint32_t fp[B];
+    if constexpr ( PK )
+    {
+#pragma unroll
+        for ( int b = 0; b < B; ++b )
+            fp[b] = ( ( w0[b] >> ( 32 - l0 ) ) << ( L - l0 ) ) | ( ( w1a[b] >> ( 32 - l1 ) ) << ( 2 * L - l1 ) ) |
+                    ( ( w1b[b] >> ( 32 - l1 ) ) << ( 3 * L - l1 ) );
+    }
 
     auto flush = [&] () {
         for ( uint32_t k = 0; k < G; ++k )
@@ -290,11 +306,24 @@ __global__ void __launch_bounds__ ( kDPThreads ) k_dp_struct1_hd ( const StructA
         for ( int r = 0; r < 32; ++r )
         {
             uint32_t Y[B];
+            if constexpr ( PK )
+            {
+                uint32_t x = 0;
 #pragma unroll
-            for ( int b = 0; b < B; ++b ) Y[b] = __funnelshift_rc ( prev[b], cur[b], r + 1 );
-            m0 |= ( uint32_t ) hd_hit<B> ( w0, Y, top0, a.e0 ) << r;
-            ma |= ( uint32_t ) hd_hit<B> ( w1a, Y, top1, a.e1 ) << r;
-            mb |= ( uint32_t ) hd_hit<B> ( w1b, Y, top1, a.e1 ) << r;
+                for ( int b = 0; b < B; ++b )
+                    x |= fp[b] ^ ( ( __funnelshift_rc ( prev[b], cur[b], r + 1 ) >> ( 32 - L ) ) * rep3 );
+                m0 |= ( uint32_t ) ( __popc ( x & mA ) <= a.e0 ) << r;
+                ma |= ( uint32_t ) ( __popc ( x & mB ) <= a.e1 ) << r;
+                mb |= ( uint32_t ) ( __popc ( x & mC ) <= a.e1 ) << r;
+            }
+            else
+            {
+#pragma unroll
+                for ( int b = 0; b < B; ++b ) Y[b] = __funnelshift_rc ( prev[b], cur[b], r + 1 );
+                m0 |= ( uint32_t ) hd_hit<B> ( w0, Y, top0, a.e0 ) << r;
+                ma |= ( uint32_t ) hd_hit<B> ( w1a, Y, top1, a.e1 ) << r;
+                mb |= ( uint32_t ) hd_hit<B> ( w1b, Y, top1, a.e1 ) << r;
+            }
         }
         if ( ! has_r1 ) mb = 0;
         X = ( ( uint64_t ) ( m0 & vm ) << 32 ) | ( X >> 32 );
@@ -721,8 +750,10 @@ static void launch_struct_b ( const StructArgs & a, bool ed, dim3 grid, size_t s
     }
     else if ( ed )
         k_dp_struct1<B, true><<<grid, kDPThreads, smem, st>>> ( a );
+    else if ( block && 3 * std::max ( a.l0, a.l1 ) <= 32 && ! getenv ( "MOTEX_STRUCT_NO_PACK" ) )
+        k_dp_struct1_hd<B, true><<<grid, kDPThreads, smem, st>>> ( a );
     else if ( block )
-        k_dp_struct1_hd<B><<<grid, kDPThreads, smem, st>>> ( a );
+        k_dp_struct1_hd<B, false><<<grid, kDPThreads, smem, st>>> ( a );
     else
         k_dp_struct1<B, false><<<grid, kDPThreads, smem, st>>> ( a );
 }

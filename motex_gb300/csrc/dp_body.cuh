@@ -389,7 +389,9 @@ __device__ __forceinline__ void dp_swar_body ( const DPArgs & a, const SwarConst
     }
     uint32_t Pv[W], Mv[W], sc[W], cnt[W];
 #pragma unroll
-    for ( int i = 0; i < W; ++i ) { Pv[i] = C.NG; Mv[i] = 0; sc[i] = C.SC0; cnt[i] = 0; }
+    // sc holds score + K per field (K added once): the hit test is then one AND
+    const uint32_t sc0k = C.SC0 + C.K;
+    for ( int i = 0; i < W; ++i ) { Pv[i] = C.NG; Mv[i] = 0; sc[i] = sc0k; cnt[i] = 0; }
     constexpr bool TAB = swar_table ( B );
     uint32_t * s_eq = smem + 3 * NF * kDPThreads;            // [code][register][thread]
     uint32_t * s_hi = s_eq + 8 * W * kDPThreads;             // B = 4, 5: [high bits][register][thread]
@@ -459,7 +461,7 @@ __device__ __forceinline__ void dp_swar_body ( const DPArgs & a, const SwarConst
         for ( int b = 0; b < B; ++b ) c |= ( ( pw[b] >> r ) & 1u ) << b;
         return c;
     };
-    auto count = [&] ( int i ) { cnt[i] += ( ~( sc[i] + C.K ) & C.HB ) >> sh; };
+    auto count = [&] ( int i ) { cnt[i] += ( ~sc[i] & C.HB ) >> sh; };
     auto drain = [&] () {                           // register fields -> shared counters
 #pragma unroll
         for ( int i = 0; i < W; ++i )
@@ -588,7 +590,7 @@ __device__ __forceinline__ void dp_swar_body ( const DPArgs & a, const SwarConst
                         cur_split = -1;
                     }
 #pragma unroll
-                    for ( int i = 0; i < W; ++i ) { Pv[i] = C.NG; Mv[i] = 0; sc[i] = C.SC0; }
+                    for ( int i = 0; i < W; ++i ) { Pv[i] = C.NG; Mv[i] = 0; sc[i] = sc0k; }
                 }
             }
         }

@@ -623,7 +623,7 @@ __global__ void __launch_bounds__ ( kDPThreads ) k_dp_struct1_swar_blk ( const S
     const uint32_t stride = a.text.plane_stride;
     const uint32_t sh = C.s;
     const uint32_t full = 0xffffffffu;
-    uint32_t Pv = C.NG, Mv = 0, sc = C.SC0;
+    uint32_t Pv = C.NG, Mv = 0, sc = C.SC0 + C.K;          // score + K per field
     uint64_t X = 0;
 
     auto flush = [&] () {
@@ -664,7 +664,7 @@ __global__ void __launch_bounds__ ( kDPThreads ) k_dp_struct1_swar_blk ( const S
             const uint32_t Ph2 = Ph << 1, Mh2 = Mhs << 1;
             Pv = Mh2 | ~( Xv | Ph2 );
             Mv = Ph2 & Xv & C.NG;
-            const uint32_t hits = ~( sc + C.K ) & C.HB;
+            const uint32_t hits = ~sc & C.HB;
             // append bit 0 of (hits >> p) at bit 31; after 32 positions bit r is position r
             m0 = __funnelshift_r ( m0, hits >> pA, 1 );
             ma = __funnelshift_r ( ma, hits >> pB, 1 );
@@ -673,7 +673,7 @@ __global__ void __launch_bounds__ ( kDPThreads ) k_dp_struct1_swar_blk ( const S
             {
                 Pv = C.NG;
                 Mv = 0;
-                sc = C.SC0;
+                sc = C.SC0 + C.K;
             }
         }
         if ( ! has_r1 ) mb = 0;

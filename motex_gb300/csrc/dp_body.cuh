@@ -496,16 +496,23 @@ __device__ __forceinline__ void dp_swar_body ( const DPArgs & a, const SwarConst
         const bool counting = k >= ch.begin;
         if ( counting && vm == 0xffffffffu && em == 0u )
         {
+            // B >= 4 (protein-like: chance hits are rare): a group of UR
+            // positions only ORs the factors' hit bits, and a group that saw one
+            // is replayed from its starting state with exact per-position counts
+            // (the steps are deterministic).  With 2-3 planes (DNA) hits are
+            // frequent enough that the replays cost what the deferral saves, so
+            // every step counts.
+            constexpr bool DEFER = B >= 4;
 #pragma unroll 1
             for ( int g = 0; g < 32; g += UR )
             {
                 uint32_t cg[B];
 #pragma unroll
                 for ( int b = 0; b < B; ++b ) cg[b] = cur[b] >> g;
-#pragma unroll
-                for ( int rr = 0; rr < UR; ++rr )
+                if constexpr ( ! DEFER )
                 {
-                    if constexpr ( TAB )
+#pragma unroll
+                    for ( int rr = 0; rr < UR; ++rr )
                     {
                         const uint32_t * row = s_eq + code_at ( cg, rr ) * ( W * kDPThreads ) + tid;
 #pragma unroll
@@ -515,27 +522,39 @@ __device__ __forceinline__ void dp_swar_body ( const DPArgs & a, const SwarConst
                             count ( i );
                         }
                     }
-                    else if constexpr ( true )
+                    continue;
+                }
+                uint32_t P0[W], M0[W], S0[W];
+#pragma unroll
+                for ( int i = 0; i < W; ++i ) { P0[i] = Pv[i]; M0[i] = Mv[i]; S0[i] = sc[i]; }
+                uint32_t hacc = 0;
+#pragma unroll
+                for ( int rr = 0; rr < UR; ++rr )
+                {
+                    const uint32_t c = code_at ( cg, rr );
+                    const uint32_t * lo = s_eq + ( TAB ? c : ( c & 7u ) ) * ( W * kDPThreads ) + tid;
+                    const uint32_t * hi = s_hi + ( c >> 3 ) * ( W * kDPThreads ) + tid;
+#pragma unroll
+                    for ( int i = 0; i < W; ++i )
+                    {
+                        step_eq ( i, TAB ? lo[i * kDPThreads] : ( lo[i * kDPThreads] & hi[i * kDPThreads] ) );
+                        hacc |= ~sc[i] & C.HB;
+                    }
+                }
+                if ( hacc )
+                {
+#pragma unroll
+                    for ( int i = 0; i < W; ++i ) { Pv[i] = P0[i]; Mv[i] = M0[i]; sc[i] = S0[i]; }
+#pragma unroll 1
+                    for ( int rr = 0; rr < UR; ++rr )
                     {
                         const uint32_t c = code_at ( cg, rr );
-                        const uint32_t * lo = s_eq + ( c & 7u ) * ( W * kDPThreads ) + tid;
+                        const uint32_t * lo = s_eq + ( TAB ? c : ( c & 7u ) ) * ( W * kDPThreads ) + tid;
                         const uint32_t * hi = s_hi + ( c >> 3 ) * ( W * kDPThreads ) + tid;
 #pragma unroll
                         for ( int i = 0; i < W; ++i )
                         {
-                            step_eq ( i, lo[i * kDPThreads] & hi[i * kDPThreads] );
-                            count ( i );
-                        }
-                    }
-                    else
-                    {
-                        uint32_t T[B];
-#pragma unroll
-                        for ( int b = 0; b < B; ++b ) T[b] = ( 0u - ( ( cg[b] >> rr ) & 1u ) ) & C.NG;
-#pragma unroll
-                        for ( int i = 0; i < W; ++i )
-                        {
-                            step ( i, T );
+                            step_eq ( i, TAB ? lo[i * kDPThreads] : ( lo[i * kDPThreads] & hi[i * kDPThreads] ) );
                             count ( i );
                         }
                     }

@@ -1,0 +1,92 @@
+"""Pin the full-size configurations to the reference itself.
+
+For each configuration below, the seeded input is generated (the same
+generators the benchmark and the GPU tests use), the reference MoTeX built by
+oracle/build_ref.sh (motexOMP, all host threads) is run on it, and the
+SHA-256 and line count of its output file -- without the two volatile header
+lines -- are stored in tests/golden/fullsize.json.  The outputs are too large
+to commit (config 2 prints 441,205 motifs); tests/test_gpu_fullsize_ref.py
+regenerates each input, runs motexGPU with the same switches and compares the
+hash.  Each reference run takes from minutes to about an hour on 8 cores;
+entries are written as they finish, and existing ones are kept unless named
+with --redo.
+
+usage: python tests/golden/make_fullsize_hashes.py [--only NAME ...] [--redo]
+"""
+from __future__ import annotations
+
+import argparse
+import hashlib
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from motex_gb300 import workloads as W  # noqa: E402
+
+OUT = os.path.join(HERE, "fullsize.json")
+REF = os.path.join(ROOT, "oracle", "_ref", "motexOMP")
+
+# name -> (workload factory, description)
+CASES = {
+    "c2_dna_ed": (lambda: W.dna_ed(), "config 2: DNA 1200 x U[800,1200], -d 1 -k 15 -e 3 -q 10"),
+    "c3_prot_d0": (lambda: W.prot_uneven(d=0), "config 3: PROT 2000 x logU[50,2000], -d 0 -k 10 -e 2 -q 15"),
+    "c3_prot_d1": (lambda: W.prot_uneven(d=1), "config 3: PROT 2000 x logU[50,2000], -d 1 -k 10 -e 2 -q 15"),
+    "c4_dna_long_tenth": (lambda: W.dna_long(scale=0.1),
+                          "config 4 at 1/10 length: DNA 8 x 100 knt with tandem repeats, -d 0 -k 20 -e 3 -q 50"),
+    "c4s_struct_d0": (lambda: W.structured(d=0), "config 4 structured on config 2's input: -k 8 -e 1 -s (5-15, 10, 1), -d 0"),
+    "c4s_struct_d1": (lambda: W.structured(d=1), "config 4 structured on config 2's input: -k 8 -e 1 -s (5-15, 10, 1), -d 1"),
+}
+
+
+def strip_volatile(text: str) -> str:
+    return "".join(l for l in text.splitlines(True)
+                   if not l.startswith(("# Rundate:", "# Run on ", "User time:")))
+
+
+def run_case(name):
+    w = CASES[name][0]()
+    with tempfile.TemporaryDirectory() as tmp:
+        W.write_fasta(os.path.join(tmp, "in.fa"), w.seqs, width=60)
+        boxes = None
+        if w.boxes:
+            boxes = "in.boxes"
+            W.write_boxes(os.path.join(tmp, boxes), w.boxes)
+        args = w.cli("in.fa", "out.motex", boxes)
+        t0 = time.time()
+        subprocess.run([REF] + args + ["-t", str(os.cpu_count())], cwd=tmp, check=True,
+                       stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+        secs = time.time() - t0
+        with open(os.path.join(tmp, "out.motex")) as f:
+            text = strip_volatile(f.read())
+    return {"args": args, "description": CASES[name][1],
+            "sha256": hashlib.sha256(text.encode()).hexdigest(),
+            "lines": text.count("\n"), "reference": "motexOMP", "threads": os.cpu_count(),
+            "reference_seconds": round(secs, 1)}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--only", nargs="*")
+    ap.add_argument("--redo", action="store_true")
+    a = ap.parse_args()
+    if not os.path.exists(REF):
+        sys.exit("make_fullsize_hashes: oracle/_ref/motexOMP missing (run oracle/build_ref.sh on x86-64)")
+    table = json.load(open(OUT)) if os.path.exists(OUT) else {}
+    for name in a.only or list(CASES):
+        if name in table and not a.redo:
+            continue
+        table[name] = run_case(name)
+        with open(OUT, "w") as f:
+            json.dump(table, f, indent=1, sort_keys=True)
+        print(name, table[name]["lines"], table[name]["reference_seconds"], "s", flush=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,5 +1,5 @@
 """bench.py's multi-GPU form runs one replica per rank ("replicas only":
-the benchmark spec fixes one GPU and the path needs no exchange step).  Its
+the engine targets one GPU and the path needs no exchange step).  Its
 host-side aggregation -- max time over ranks, work summed over ranks -- is
 checked here with two gloo ranks on the CPU."""
 import os

@@ -169,7 +169,8 @@ bool launch_dp_hswar ( const DPArgs & a, int B, int NL, int W, int UR, dim3 grid
 // Register words per thread of the packed kernels when the shape is not tuned
 // (batched jobs, persistent launches, the default of an untuned job): with
 // B = 4, 5 the split Eq table leaves room for enough CTAs per SM only at
-// W = 4 (measured on config 3: W = 4 runs 352 ms, W = 8 393 ms).
+// W = 4 (measured on 2000 protein sequences of 50-2000 residues, edit
+// distance, k 10: W = 4 runs 352 ms, W = 8 393 ms).
 __host__ __device__ constexpr int swar_default_w ( int B ) { return B >= 4 ? 4 : 8; }
 
 // One job of a batched launch and one unit of its work.

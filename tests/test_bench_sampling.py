@@ -1,0 +1,32 @@
+"""bench.py's CPU-baseline sample is bounded by symbols: on a workload of a
+few very long sequences it must not start from whole sequences (a run that
+is quadratic in 16 M symbols never ends).  A fake CPU run whose time grows
+with the square of the symbols stands in for the real one."""
+import bench
+from motex_gb300 import workloads as W
+
+
+def test_sample_is_bounded_in_symbols(monkeypatch):
+    calls = []
+
+    def fake_run(binary, wl, seqs, threads, timeout=600):
+        n = sum(map(len, seqs))
+        calls.append(n)
+        secs = (n / 50_000.0) ** 2            # 50k symbols per second squared
+        return n * n, secs
+
+    monkeypatch.setattr(bench, "cpu_run", fake_run)
+    wl = W.Workload("long", "DNA", ["ACGT" * 250_000] * 16, d=0, k=12, e=1, q=50)   # 16 x 1 Mnt
+    sample, desc = bench.cpu_sample("x", wl, 8, target_s=12.0)
+    assert calls[0] <= 20_000                               # the first probe is small
+    assert all(b <= 2 * a for a, b in zip(calls, calls[1:]))  # and grows geometrically
+    total = sum(map(len, sample))
+    assert 100_000 < total < 300_000                        # ~sqrt(12) x 50k symbols
+    assert "the last cut to" in desc and "of 16 sequences" in desc
+
+
+def test_sample_takes_whole_set_when_cheap(monkeypatch):
+    monkeypatch.setattr(bench, "cpu_run", lambda b, wl, seqs, t, timeout=600: (1, 0.001))
+    wl = W.Workload("small", "DNA", ["ACGTACGTAC"] * 5, d=0, k=4, e=0, q=50)
+    sample, desc = bench.cpu_sample("x", wl, 8)
+    assert sample == wl.seqs

@@ -12,9 +12,12 @@
 //    the top l bits; hit = popc <= e.
 //  Edit distance (d = 1), flasm_ed contract: a hit ends at p when
 //    min_s ED(factor, t[s..p]) <= e.  Myers/Hyyro bit-vector column recurrence
-//    (one 32-bit word per factor, l <= 32), Eq built from the factor planes
-//    and the broadcast text symbol bits; the score D[l][p] is tracked either
-//    scaled by 2^(l-1) (l <= 28, two ANDs and one add) or shifted down.
+//    (one 32-bit word per factor, l <= 32, or 2-4 factors per word for
+//    l <= 15); Eq is read from a per-thread table by the text symbol's code
+//    (B <= 3; split into low and high code bits for B = 4, 5 in the packed
+//    body) or built from the factor planes and the broadcast text symbol
+//    bits; the score D[l][p] is tracked either scaled by 2^(l-1) (l <= 28,
+//    two ANDs and one add) or shifted down.
 //
 // Per (factor, sequence): hits are counted; at the end of each sequence the
 // count goes to v and (count > 0) to u.  A sequence cut by a chunk boundary
@@ -388,9 +391,9 @@ __device__ __forceinline__ void dp_swar_body ( const DPArgs & a, const SwarConst
         }
     }
     uint32_t Pv[W], Mv[W], sc[W], cnt[W];
-#pragma unroll
     // sc holds score + K per field (K added once): the hit test is then one AND
     const uint32_t sc0k = C.SC0 + C.K;
+#pragma unroll
     for ( int i = 0; i < W; ++i ) { Pv[i] = C.NG; Mv[i] = 0; sc[i] = sc0k; cnt[i] = 0; }
     constexpr bool TAB = swar_table ( B );
     uint32_t * s_eq = smem + 3 * NF * kDPThreads;            // [code][register][thread]
@@ -447,12 +450,6 @@ __device__ __forceinline__ void dp_swar_body ( const DPArgs & a, const SwarConst
         const uint32_t Ph2 = Ph << 1, Mh2 = Mhs << 1;
         Pv[i] = Mh2 | ~( Xv | Ph2 );
         Mv[i] = Ph2 & Xv & C.NG;
-    };
-    auto step = [&] ( int i, const uint32_t ( &T )[B] ) {
-        uint32_t x = wp[i][0] ^ T[0];
-#pragma unroll
-        for ( int b = 1; b < B; ++b ) x |= wp[i][b] ^ T[b];
-        step_eq ( i, ~x );
     };
     // code of text position r from the plane words (bit b of the code in plane b)
     auto code_at = [&] ( const uint32_t ( &pw )[B], int r ) {
@@ -522,8 +519,9 @@ __device__ __forceinline__ void dp_swar_body ( const DPArgs & a, const SwarConst
                             count ( i );
                         }
                     }
-                    continue;
                 }
+                else
+                {
                 uint32_t P0[W], M0[W], S0[W];
 #pragma unroll
                 for ( int i = 0; i < W; ++i ) { P0[i] = Pv[i]; M0[i] = Mv[i]; S0[i] = sc[i]; }
@@ -559,6 +557,7 @@ __device__ __forceinline__ void dp_swar_body ( const DPArgs & a, const SwarConst
                         }
                     }
                 }
+                }
             }
         }
         else
@@ -576,7 +575,7 @@ __device__ __forceinline__ void dp_swar_body ( const DPArgs & a, const SwarConst
                         if ( count_here ) count ( i );
                     }
                 }
-                else if constexpr ( true )
+                else
                 {
                     const uint32_t c = code_at ( cur, r );
                     const uint32_t * lo = s_eq + ( c & 7u ) * ( W * kDPThreads ) + tid;
@@ -585,18 +584,6 @@ __device__ __forceinline__ void dp_swar_body ( const DPArgs & a, const SwarConst
                     for ( int i = 0; i < W; ++i )
                     {
                         step_eq ( i, lo[i * kDPThreads] & hi[i * kDPThreads] );
-                        if ( count_here ) count ( i );
-                    }
-                }
-                else
-                {
-                    uint32_t T[B];
-#pragma unroll
-                    for ( int b = 0; b < B; ++b ) T[b] = ( 0u - ( ( cur[b] >> r ) & 1u ) ) & C.NG;
-#pragma unroll
-                    for ( int i = 0; i < W; ++i )
-                    {
-                        step ( i, T );
                         if ( count_here ) count ( i );
                     }
                 }

@@ -198,10 +198,14 @@ bool launch_dp_fast ( const DPArgs & a, int B, int W, int UR, bool ed, dim3 grid
     }
 }
 
+// Lane stride: l symbols, a guard bit, and for l = 4 a spare bit, so that
+// every S-bit count field holds the 32 hits of one text block.
+static uint32_t swar_stride ( uint32_t l ) { return std::max ( l + 1, 6u ); }
+
 int swar_lanes ( uint32_t l )
 {
     if ( l < 4 || l > 15 ) return 1;
-    return std::min ( 4, 33 / ( int ) ( l + 1 ) );
+    return std::min ( 4, ( int ) ( ( 32 - l ) / swar_stride ( l ) ) + 1 );
 }
 
 template <int B, int NL, int W>
@@ -247,21 +251,23 @@ static bool launch_swar_b ( const DPArgs & a, const SwarConst & C, int NL, int W
 
 SwarConst swar_const ( uint32_t l, uint32_t e, int NL )
 {
-    SwarConst C;
-    C.S = l + 1;
-    C.HB = C.NG = C.K = C.SC0 = 0;
+    SwarConst C {};
+    C.S = swar_stride ( l );
     uint32_t guards = 0;
     for ( int j = 0; j < NL; ++j )
     {
         const uint32_t o = j * C.S;
         C.HB |= 1u << ( o + l - 1 );
-        if ( o + l < 32 ) guards |= 1u << ( o + l );
+        for ( uint32_t g = o + l; g < o + C.S && g < 32; ++g ) guards |= 1u << g;
         C.K += ( ( 1u << ( l - 1 ) ) - ( e + 1 ) ) << o;
         C.SC0 += l << o;
     }
     C.NG = ~guards;
     C.NGm1 = C.NG & ~C.HB;
     C.FM = ( 1u << C.S ) - 1u;
+    C.ONE = 1u;
+    C.TWO = 2u;
+    C.NEG1 = ~0u;
     return C;
 }
 

@@ -330,14 +330,19 @@ __device__ __forceinline__ bool next_item ( const WorkItem * items, uint32_t nit
 
 /*
  * Edit distance with NL factors per 32-bit register (SWAR), l <= 15.
- * Lane i holds a factor in bits [i*S, i*S+l), S = l+1, with a guard bit at
- * i*S+l.  The text bits are cleared at the guards, so Eq has 1 there; Pv and
+ * Lane i holds a factor in bits [i*S, i*S+l), S = max(l+1, 6), with guard
+ * bits from i*S+l up to the next lane (S >= 6 lets every S-bit count field
+ * hold the 32 hits of one text block).  The text bits are cleared at the
+ * guards, so Eq has 1 there; Pv and
  * Mv keep 0 there (Mv through the NG mask, Pv because the Mh that is shifted
  * up is taken without the lanes' top bits).  With those invariants no carry
  * of (Eq&Pv)+Pv and no shifted Ph/Mh bit crosses into the next lane.  The
  * per-lane scores live in bit fields at i*S (each in [0, l]); the hit test
  * adds 2^(l-1)-(e+1) per field and reads bit l-1 of each field.  Hits are
  * counted in per-lane fields and moved to shared memory every 32 positions.
+ * The step is bound by the ALU pipe (logic ops, shifts, adds); its adds and
+ * left shifts are written as multiply-adds by runtime constants so that they
+ * issue on the otherwise idle FMA pipe.
  */
 
 /*
@@ -439,15 +444,18 @@ __device__ __forceinline__ void dp_swar_body ( const DPArgs & a, const SwarConst
     const uint32_t stride = a.text.plane_stride;
 
     auto step_eq = [&] ( int i, const uint32_t Eq ) {
+        // additions and left shifts as multiply-adds by runtime constants:
+        // they run on the FMA pipe, which the logic ops leave idle
         const uint32_t Xv = Eq | Mv[i];
-        const uint32_t s = ( Eq & Pv[i] ) + Pv[i];
+        const uint32_t s = ( Eq & Pv[i] ) * C.ONE + Pv[i];
         const uint32_t Xh = ( s ^ Pv[i] ) | Eq;
         const uint32_t Ph = Mv[i] | ~( Xh | Pv[i] );
         const uint32_t Mhs = Pv[i] & Xh & C.NGm1;
         const uint32_t mh = Pv[i] & Xh & C.HB;
         const uint32_t ph = Ph & C.HB;
-        sc[i] = sc[i] + ( ph >> sh ) - ( mh >> sh );
-        const uint32_t Ph2 = Ph << 1, Mh2 = Mhs << 1;
+        sc[i] = ( ph >> sh ) * C.ONE + sc[i];
+        sc[i] = ( mh >> sh ) * C.NEG1 + sc[i];
+        const uint32_t Ph2 = Ph * C.TWO, Mh2 = Mhs * C.TWO;
         Pv[i] = Mh2 | ~( Xv | Ph2 );
         Mv[i] = Ph2 & Xv & C.NG;
     };
@@ -458,7 +466,7 @@ __device__ __forceinline__ void dp_swar_body ( const DPArgs & a, const SwarConst
         for ( int b = 0; b < B; ++b ) c |= ( ( pw[b] >> r ) & 1u ) << b;
         return c;
     };
-    auto count = [&] ( int i ) { cnt[i] += ( ~sc[i] & C.HB ) >> sh; };
+    auto count = [&] ( int i ) { cnt[i] = ( ( ~sc[i] & C.HB ) >> sh ) * C.ONE + cnt[i]; };
     auto drain = [&] () {                           // register fields -> shared counters
 #pragma unroll
         for ( int i = 0; i < W; ++i )

@@ -56,6 +56,17 @@ __device__ __forceinline__ bool hd_hit ( const uint32_t ( &w )[B], const uint32_
     return __popc ( x & mask ) <= e;
 }
 
+// 1 when popc(x & mask) <= e, with ne = -(e+1): the sign bit of a multiply-add
+template <int B>
+__device__ __forceinline__ uint32_t hd_hitbit ( const uint32_t ( &w )[B], const uint32_t ( &Y )[B], uint32_t mask,
+                                                uint32_t one, uint32_t ne )
+{
+    uint32_t x = ( w[0] ^ Y[0] );
+#pragma unroll
+    for ( int b = 1; b < B; ++b ) x |= w[b] ^ Y[b];
+    return ( __popc ( x & mask ) * one + ne ) >> 31;
+}
+
 } // namespace
 
 template <int B, bool ED>
@@ -261,6 +272,7 @@ __global__ void __launch_bounds__ ( kDPThreads ) k_dp_struct1_hd ( const StructA
     const uint32_t top0 = l0 >= 32 ? 0xffffffffu : ~( ( 1u << ( 32 - l0 ) ) - 1u );
     const uint32_t top1 = l1 >= 32 ? 0xffffffffu : ~( ( 1u << ( 32 - l1 ) ) - 1u );
     const uint32_t full = 0xffffffffu;
+    const uint32_t one = a.one, two = a.one << 1, ne0 = a.ne0, ne1 = a.ne1;
     // PK: the three rows as lanes of L = max(l0, l1) <= 10 bits of one register
     // (box 0, row r0, row r1), each factor in the top of its lane; the window's
     // newest L symbols are replicated into the lanes by a multiply
@@ -301,6 +313,8 @@ __global__ void __launch_bounds__ ( kDPThreads ) k_dp_struct1_hd ( const StructA
         for ( int b = 0; b < B; ++b ) cur[b] = __ldg ( planes + ( size_t ) b * stride + kb + 1 );
         const uint32_t vm = __ldg ( a.text.vmask + kb ), em = __ldg ( a.text.emask + kb );
         const bool counting = kb >= ch.begin;
+        // hit masks built in reverse bit order (position r at bit 31-r) as
+        // m * 2 + hit, multiply-adds on the FMA pipe; one bit reversal per block
         uint32_t m0 = 0, ma = 0, mb = 0;
 #pragma unroll 8
         for ( int r = 0; r < 32; ++r )
@@ -312,19 +326,22 @@ __global__ void __launch_bounds__ ( kDPThreads ) k_dp_struct1_hd ( const StructA
 #pragma unroll
                 for ( int b = 0; b < B; ++b )
                     x |= fp[b] ^ ( ( __funnelshift_rc ( prev[b], cur[b], r + 1 ) >> ( 32 - L ) ) * rep3 );
-                m0 |= ( uint32_t ) ( __popc ( x & mA ) <= a.e0 ) << r;
-                ma |= ( uint32_t ) ( __popc ( x & mB ) <= a.e1 ) << r;
-                mb |= ( uint32_t ) ( __popc ( x & mC ) <= a.e1 ) << r;
+                m0 = m0 * two + ( ( __popc ( x & mA ) * one + ne0 ) >> 31 );
+                ma = ma * two + ( ( __popc ( x & mB ) * one + ne1 ) >> 31 );
+                mb = mb * two + ( ( __popc ( x & mC ) * one + ne1 ) >> 31 );
             }
             else
             {
 #pragma unroll
                 for ( int b = 0; b < B; ++b ) Y[b] = __funnelshift_rc ( prev[b], cur[b], r + 1 );
-                m0 |= ( uint32_t ) hd_hit<B> ( w0, Y, top0, a.e0 ) << r;
-                ma |= ( uint32_t ) hd_hit<B> ( w1a, Y, top1, a.e1 ) << r;
-                mb |= ( uint32_t ) hd_hit<B> ( w1b, Y, top1, a.e1 ) << r;
+                m0 = m0 * two + hd_hitbit<B> ( w0, Y, top0, one, ne0 );
+                ma = ma * two + hd_hitbit<B> ( w1a, Y, top1, one, ne1 );
+                mb = mb * two + hd_hitbit<B> ( w1b, Y, top1, one, ne1 );
             }
         }
+        m0 = __brev ( m0 );
+        ma = __brev ( ma );
+        mb = __brev ( mb );
         if ( ! has_r1 ) mb = 0;
         X = ( ( uint64_t ) ( m0 & vm ) << 32 ) | ( X >> 32 );
         // positions where some lane's box-1 row hits: OR over the warp by a
@@ -400,6 +417,10 @@ struct HSwarConst
     uint32_t HB, NG, NGm1, K, SC0, s;
     uint32_t bitA, bitB, bitC;      // top bit of box 0, row r0, row r1
     uint32_t oB, oC;
+    // multipliers (runtime values: multiply-adds issue on the FMA pipe):
+    // 1, 2, -1, and -2^(31-p) for the top bit p of each lane, so that
+    // (sc * nm + nm) >> 31 = bit p of ~sc
+    uint32_t one, two, neg1, nmA, nmB, nmC;
 };
 
 bool hswar_shape ( const StructArgs & a, HSwarConst * C )
@@ -429,6 +450,12 @@ bool hswar_shape ( const StructArgs & a, HSwarConst * C )
     C->bitC = 1u << ( oC + a.b1 - 1 );
     C->oB = oB;
     C->oC = oC;
+    C->one = 1u;
+    C->two = 2u;
+    C->neg1 = ~0u;
+    C->nmA = 0u - ( 1u << ( 31 - ( a.l0 - 1 ) ) );
+    C->nmB = 0u - ( 1u << ( 31 - ( oB + a.b1 - 1 ) ) );
+    C->nmC = 0u - ( 1u << ( 31 - ( oC + a.b1 - 1 ) ) );
     return true;
 }
 
@@ -615,8 +642,6 @@ __global__ void __launch_bounds__ ( kDPThreads ) k_dp_struct1_swar_blk ( const S
     const uint32_t Gmask = G >= 32 ? 0xffffffffu : ( ( 1u << G ) - 1u );
     const uint32_t lo = a.gmin + a.b1, hi = a.gmax + a.b1;            // hi <= 31 (launch check)
     const uint32_t wmask = hi - lo + 1 >= 32 ? 0xffffffffu : ( ( 1u << ( hi - lo + 1 ) ) - 1u );
-    // bit positions of the three lanes' top bits: box 0 < row r0 < row r1
-    const uint32_t pA = __ffs ( C.bitA ) - 1, pB = __ffs ( C.bitB ) - 1, pC = __ffs ( C.bitC ) - 1;
     const ChunkInfo ch = a.chunks[blockIdx.y];
     int cur_split = ch.first_split;
     const uint32_t * __restrict__ planes = a.text.planes;
@@ -645,37 +670,53 @@ __global__ void __launch_bounds__ ( kDPThreads ) k_dp_struct1_swar_blk ( const S
         for ( int b = 0; b < B; ++b ) cur[b] = __ldg ( planes + ( size_t ) b * stride + kb + 1 );
         const uint32_t vm = __ldg ( a.text.vmask + kb ), em = __ldg ( a.text.emask + kb );
         const bool counting = kb >= ch.begin;
+        // hit masks built in reverse bit order (position r at bit 31-r) as
+        // m * 2 + hit; adds, left shifts and the hit-bit extraction are
+        // multiply-adds (FMA pipe), the logic ops of the step fill the ALU
         uint32_t m0 = 0, ma = 0, mb = 0;
-#pragma unroll 4
-        for ( int r = 0; r < 32; ++r )
-        {
+        auto step = [&] ( int r ) {
             uint32_t c = 0;
 #pragma unroll
             for ( int b = 0; b < B; ++b ) c |= ( ( cur[b] >> r ) & 1u ) << b;
             const uint32_t Eq = s_eq[c * kDPThreads + threadIdx.x];
             const uint32_t Xv = Eq | Mv;
-            const uint32_t s1 = ( Eq & Pv ) + Pv;
+            const uint32_t s1 = ( Eq & Pv ) * C.one + Pv;
             const uint32_t Xh = ( s1 ^ Pv ) | Eq;
             const uint32_t Ph = Mv | ~( Xh | Pv );
             const uint32_t Mhs = Pv & Xh & C.NGm1;
             const uint32_t mh = Pv & Xh & C.HB;
             const uint32_t ph = Ph & C.HB;
-            sc = sc + ( ph >> sh ) - ( mh >> sh );
-            const uint32_t Ph2 = Ph << 1, Mh2 = Mhs << 1;
+            sc = ( ph >> sh ) * C.one + sc;
+            sc = ( mh >> sh ) * C.neg1 + sc;
+            const uint32_t Ph2 = Ph * C.two, Mh2 = Mhs * C.two;
             Pv = Mh2 | ~( Xv | Ph2 );
             Mv = Ph2 & Xv & C.NG;
-            const uint32_t hits = ~sc & C.HB;
-            // append bit 0 of (hits >> p) at bit 31; after 32 positions bit r is position r
-            m0 = __funnelshift_r ( m0, hits >> pA, 1 );
-            ma = __funnelshift_r ( ma, hits >> pB, 1 );
-            mb = __funnelshift_r ( mb, hits >> pC, 1 );
-            if ( ( em >> r ) & 1u )
+            m0 = m0 * C.two + ( ( sc * C.nmA + C.nmA ) >> 31 );
+            ma = ma * C.two + ( ( sc * C.nmB + C.nmB ) >> 31 );
+            mb = mb * C.two + ( ( sc * C.nmC + C.nmC ) >> 31 );
+        };
+        if ( em == 0u )
+        {
+#pragma unroll 4
+            for ( int r = 0; r < 32; ++r ) step ( r );
+        }
+        else
+        {
+#pragma unroll 4
+            for ( int r = 0; r < 32; ++r )
             {
-                Pv = C.NG;
-                Mv = 0;
-                sc = C.SC0 + C.K;
+                step ( r );
+                if ( ( em >> r ) & 1u )
+                {
+                    Pv = C.NG;
+                    Mv = 0;
+                    sc = C.SC0 + C.K;
+                }
             }
         }
+        m0 = __brev ( m0 );
+        ma = __brev ( ma );
+        mb = __brev ( mb );
         if ( ! has_r1 ) mb = 0;
         X = ( ( uint64_t ) ( m0 & vm ) << 32 ) | ( X >> 32 );
         uint32_t R = ma | mb;

@@ -92,6 +92,10 @@ struct StructArgs
     uint32_t          l1, e1;        // box 1 (l1 = b1)
     uint32_t          b1;
     uint32_t          gmin, gmax, G; // gap range, G = gmax - gmin + 1
+    // 1, -(e0+1), -(e1+1): the Hamming kernels take a hit as the sign bit of
+    // popc * one - (e+1) and shift it into their masks with multiply-adds
+    // (FMA pipe; runtime values the compiler cannot fold)
+    uint32_t          one, ne0, ne1;
     const ChunkInfo * chunks;
     uint32_t *        u_acc;         // [pos * G + k]
     uint32_t *        v_acc;
@@ -158,6 +162,11 @@ struct SwarConst
     uint32_t S;      // lane stride
     uint32_t FM;     // field mask (S bits)
     uint32_t REP;    // Hamming lanes: sum of 2^(j*l), replicates an l-bit window into every lane
+    // Multipliers of the edit-distance step, kernel parameters so that the
+    // compiler cannot fold them: x * ONE + y, x * TWO and x * NEG1 + y run as
+    // integer multiply-adds on the FMA pipe instead of adds and shifts on
+    // the ALU pipe, which the logic ops already fill
+    uint32_t ONE, TWO, NEG1;
 };
 SwarConst swar_const ( uint32_t l, uint32_t e, int NL );
 // Hamming with NL = hswar_lanes(l) >= 2 factors of l bits per register

@@ -871,6 +871,9 @@ int plan_structured ( Job * j )
     sa.e0 = P.e;
     sa.l1 = b1;
     sa.e1 = e1;
+    sa.one = 1u;
+    sa.ne0 = ~P.e;
+    sa.ne1 = ~e1;
     sa.b1 = b1;
     sa.gmin = gmin;
     sa.gmax = gmax;

@@ -53,6 +53,25 @@ def test_random_whole_set(native_built, oracle_port, seed):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("kind,l,e", [("DNA", 4, 3), ("DNA", 4, 2), ("PROT", 4, 3), ("USR", 4, 3),
+                                      ("DNA", 5, 4), ("PROT", 5, 3)])
+def test_short_factors_dense_hits(native_built, oracle_port, kind, l, e):
+    """Short factors with many errors hit at nearly every text position:
+    the count field of each packed edit-distance lane must hold all 32 hits
+    of a text block without carrying into its neighbour."""
+    rng = random.Random(77 + l * 10 + e)
+    letters = {"DNA": "ACGT", "PROT": W.AMINO20, "USR": "0123456789"}[kind]
+    seqs = ["".join(rng.choice(letters) for _ in range(rng.randint(60, 700))) for _ in range(9)]
+    args = ["-a", kind, "-i", "in.fa", "-o", "out.motex", "-d", "1", "-k", str(l), "-e", str(e), "-q", "30"]
+    files = {"in.fa": fasta(seqs)}
+    g = run_cli(native_built.CLI_PATH, None, args, files=files)
+    o = run_cli(oracle_port, None, args + ["-t", "8"], files=files)
+    assert g[0] == o[0] == 0, g[2] + o[2]
+    assert g[1] == o[1]
+    assert g[1].count("\n") > 20
+
+
+@pytest.mark.gpu
 @pytest.mark.parametrize("d", [0, 1])
 def test_long_sequences_split_across_chunks(native_built, oracle_port, d):
     """Few long sequences: the DP cuts every sequence into several text

@@ -50,6 +50,7 @@ from motex_gb300 import workloads as W  # noqa: E402
 
 WORKLOADS = {
     "dna_ed": lambda s: W.dna_ed(scale=s),
+    "dna_ed_k20": lambda s: W.dna_ed(scale=s, k=20, e=4),
     "dna_hd_small": lambda s: W.dna_hd_small(scale=s),
     "prot_uneven_d0": lambda s: W.prot_uneven(d=0, scale=s),
     "prot_uneven_d1": lambda s: W.prot_uneven(d=1, scale=s),
@@ -428,6 +429,10 @@ def run_gpu(args, rank, world, local_rank):
                 "traffic": tr,
                 "note": "algorithmic ops per cell; SWAR lanes (2-4 cells per instruction) and the shared Eq "
                         "table execute fewer, so frac can exceed 1"}
+    if wl.d == 0 and not wl.boxes and dp_s > 0 and popc:
+        # plain Hamming runs one population count per cell: its second roof
+        popc_rate = first.unique_words * total_pos / dp_s / 1e12
+        roofline.update(popc_achieved=round(popc_rate, 3), popc_frac=round(popc_rate / popc, 4))
 
     extras = {}
     if rank == 0 and not args.no_extras and args.scale == 1.0:

@@ -59,6 +59,10 @@ struct DPArgs
     uint32_t          U;
     uint32_t          l;
     uint32_t          e;
+    // 1, 2 and -1 as kernel data: the edit-distance step multiplies by them
+    // (x * one + y, x * two, x * neg1 + y) so that its adds and shifts issue
+    // as multiply-adds on the FMA pipe; the compiler cannot fold them back
+    uint32_t          one, two, neg1;
     const ChunkInfo * chunks;
     uint32_t *        u_acc;
     uint32_t *        v_acc;

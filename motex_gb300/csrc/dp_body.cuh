@@ -195,19 +195,27 @@ __device__ __forceinline__ void dp_fast_body ( const DPArgs & a, uint32_t tile, 
                     for ( int b = 0; b < B; ++b ) x |= wp[i][b] ^ ( ( ( c >> b ) & 1 ) ? 0xffffffffu : 0u );
                     s_eq[( c * W + i ) * kDPThreads + threadIdx.x] = ~x;
                 }
+        // adds and shifts as multiply-adds by 1, 2 and -1 held in kernel data:
+        // they issue on the FMA pipe, which the step's logic ops leave idle
+        const uint32_t one = a.one, two = a.two, neg1 = a.neg1;
         auto step_eq = [&] ( int i, const uint32_t Eq ) {
             const uint32_t Xv = Eq | Mv[i];
-            const uint32_t Xh = ( ( ( Eq & Pv[i] ) + Pv[i] ) ^ Pv[i] ) | Eq;
-            uint32_t Ph = Mv[i] | ~( Xh | Pv[i] );
-            uint32_t Mh = Pv[i] & Xh;
+            const uint32_t Xh = ( ( ( Eq & Pv[i] ) * one + Pv[i] ) ^ Pv[i] ) | Eq;
+            const uint32_t Ph = Mv[i] | ~( Xh | Pv[i] );
+            const uint32_t Mh = Pv[i] & Xh;
             if constexpr ( SCALED )
-                sc[i] += ( Ph & hb ) - ( Mh & hb );
+            {
+                sc[i] = ( Ph & hb ) * one + sc[i];
+                sc[i] = ( Mh & hb ) * neg1 + sc[i];
+            }
             else
-                sc[i] += ( ( Ph >> sh ) & 1u ) - ( ( Mh >> sh ) & 1u );
-            Ph <<= 1;
-            Mh <<= 1;
-            Pv[i] = Mh | ~( Xv | Ph );
-            Mv[i] = Ph & Xv;
+            {
+                sc[i] = ( ( Ph >> sh ) & 1u ) * one + sc[i];
+                sc[i] = ( ( Mh >> sh ) & 1u ) * neg1 + sc[i];
+            }
+            const uint32_t Ph2 = Ph * two, Mh2 = Mh * two;
+            Pv[i] = Mh2 | ~( Xv | Ph2 );
+            Mv[i] = Ph2 & Xv;
         };
         auto step = [&] ( int i, const uint32_t ( &T )[B] ) {
             uint32_t x = wp[i][0] ^ T[0];

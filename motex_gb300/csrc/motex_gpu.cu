@@ -731,6 +731,9 @@ int stage_plan ( Job * j, bool sorted )
     da.U = U;
     da.l = P.l;
     da.e = P.e;
+    da.one = 1u;
+    da.two = 2u;
+    da.neg1 = ~0u;
     if ( ! j->replaying ) j->tune = choose_tune ( j, U, ed, j->generic );
     bool tune_now = false;
     if ( ! j->replaying && ! j->generic && ! j->batched && ! getenv ( "MOTEX_DP_W" ) && ! getenv ( "MOTEX_DP_UR" ) &&

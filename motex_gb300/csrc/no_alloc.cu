@@ -242,6 +242,9 @@ extern "C" int motex_gpu_extract_pair_static ( const motex_params * prm, const c
     da.U = U;
     da.l = l;
     da.e = prm->e;
+    da.one = 1u;
+    da.two = 2u;
+    da.neg1 = ~0u;
     da.chunks = chunks;
     da.u_acc = u_acc;
     da.v_acc = v_acc;

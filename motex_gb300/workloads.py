@@ -11,7 +11,8 @@ Workloads (sizes as run by ``bench.py`` and the tests):
   substitutions in 50% of sequences; ``-d 0 -k 12 -e 2 -q 50``.
 * ``dna_ed``         1200 x U[800,1200] nt, GC 40%, three 15-mers planted with
   0-3 edits (sub/ins/del equiprobable) in 20/40/60% of sequences;
-  ``-d 1 -k 15 -e 3 -q 10``.
+  ``-d 1 -k 15 -e 3 -q 10``.  ``dna_ed_k20``: the same with 20-mers and
+  ``-k 20 -e 4`` (factors of one 32-bit word, past the packed lanes).
 * ``prot_uneven``    2000 x logU[50,2000] aa over 20 amino acids with
   Dirichlet(5) frequencies, five 10-mers planted with 0-2 substitutions in
   U[15,50]% of sequences; ``-k 10 -e 2 -q 15`` with ``-d 0`` and ``-d 1``.
@@ -132,15 +133,16 @@ def dna_hd_small(seed: int = 1, scale: float = 1.0) -> Workload:
     return Workload("dna_hd_small", "DNA", seqs, d=0, k=12, e=2, q=50)
 
 
-def dna_ed(seed: int = 2, scale: float = 1.0, d: int = 1) -> Workload:
+def dna_ed(seed: int = 2, scale: float = 1.0, d: int = 1, k: int = 15, e: int = 3) -> Workload:
     rng = np.random.default_rng(seed)
     nseq = max(4, int(round(1200 * scale)))
     p = [0.3, 0.2, 0.2, 0.3]                      # A C G T, GC = 40%
     seqs = [_rand_seq(rng, DNA, int(rng.integers(800, 1201)), p) for _ in range(nseq)]
     for frac in (0.2, 0.4, 0.6):
-        motif = _rand_seq(rng, DNA, 15)
-        _plant(rng, seqs, lambda: _edit(rng, motif, DNA, int(rng.integers(4))), frac)
-    return Workload("dna_ed", "DNA", seqs, d=d, k=15, e=3, q=10)
+        motif = _rand_seq(rng, DNA, k)
+        _plant(rng, seqs, lambda: _edit(rng, motif, DNA, int(rng.integers(e + 1))), frac)
+    name = "dna_ed" if (k, e) == (15, 3) else f"dna_ed_k{k}"
+    return Workload(name, "DNA", seqs, d=d, k=k, e=e, q=10)
 
 
 def prot_uneven(seed: int = 3, scale: float = 1.0, d: int = 0) -> Workload:

@@ -467,13 +467,14 @@ __device__ __forceinline__ void dp_swar_body ( const DPArgs & a, const SwarConst
         Pv[i] = Mh2 | ~( Xv | Ph2 );
         Mv[i] = Ph2 & Xv & C.NG;
     };
-    // code of text position r from the plane words (bit b of the code in plane b)
-    auto code_at = [&] ( const uint32_t ( &pw )[B], int r ) {
-        uint32_t c = 0;
-#pragma unroll
-        for ( int b = 0; b < B; ++b ) c |= ( ( pw[b] >> r ) & 1u ) << b;
-        return c;
-    };
+    // Eq-table rows of the text positions of a block: every thread of the CTA
+    // walks the same positions, so the rows (code * W * kDPThreads; for
+    // B = 4, 5 those of the low three code bits and of the high bits) are
+    // computed once per block into shared memory, double-buffered so that one
+    // barrier per block suffices, instead of from the bit planes by every thread
+    __shared__ uint32_t s_rl[2][32], s_rh[2][32];
+    const uint32_t * my_eq = s_eq + tid;
+    const uint32_t * my_hi = s_hi + tid;
     auto count = [&] ( int i ) { cnt[i] = ( ( ~sc[i] & C.HB ) >> sh ) * C.ONE + cnt[i]; };
     auto drain = [&] () {                           // register fields -> shared counters
 #pragma unroll
@@ -502,9 +503,17 @@ __device__ __forceinline__ void dp_swar_body ( const DPArgs & a, const SwarConst
 
     for ( uint32_t k = ch.warm; k < ch.end; ++k )
     {
-        uint32_t cur[B];
+        uint32_t * rl = s_rl[( k - ch.warm ) & 1];
+        uint32_t * rh = s_rh[( k - ch.warm ) & 1];
+        if ( tid < 32 )
+        {
+            uint32_t c = 0;
 #pragma unroll
-        for ( int b = 0; b < B; ++b ) cur[b] = __ldg ( planes + ( size_t ) b * stride + k + 1 );
+            for ( int b = 0; b < B; ++b ) c |= ( ( __ldg ( planes + ( size_t ) b * stride + k + 1 ) >> tid ) & 1u ) << b;
+            rl[tid] = ( TAB ? c : ( c & 7u ) ) * ( W * kDPThreads );
+            rh[tid] = ( c >> 3 ) * ( W * kDPThreads );
+        }
+        __syncthreads ();
         const uint32_t vm = __ldg ( a.text.vmask + k ), em = __ldg ( a.text.emask + k );
         const bool counting = k >= ch.begin;
         if ( counting && vm == 0xffffffffu && em == 0u )
@@ -519,15 +528,12 @@ __device__ __forceinline__ void dp_swar_body ( const DPArgs & a, const SwarConst
 #pragma unroll 1
             for ( int g = 0; g < 32; g += UR )
             {
-                uint32_t cg[B];
-#pragma unroll
-                for ( int b = 0; b < B; ++b ) cg[b] = cur[b] >> g;
                 if constexpr ( ! DEFER )
                 {
 #pragma unroll
                     for ( int rr = 0; rr < UR; ++rr )
                     {
-                        const uint32_t * row = s_eq + code_at ( cg, rr ) * ( W * kDPThreads ) + tid;
+                        const uint32_t * row = my_eq + rl[g + rr];
 #pragma unroll
                         for ( int i = 0; i < W; ++i )
                         {
@@ -545,9 +551,8 @@ __device__ __forceinline__ void dp_swar_body ( const DPArgs & a, const SwarConst
 #pragma unroll
                 for ( int rr = 0; rr < UR; ++rr )
                 {
-                    const uint32_t c = code_at ( cg, rr );
-                    const uint32_t * lo = s_eq + ( TAB ? c : ( c & 7u ) ) * ( W * kDPThreads ) + tid;
-                    const uint32_t * hi = s_hi + ( c >> 3 ) * ( W * kDPThreads ) + tid;
+                    const uint32_t * lo = my_eq + rl[g + rr];
+                    const uint32_t * hi = my_hi + rh[g + rr];
 #pragma unroll
                     for ( int i = 0; i < W; ++i )
                     {
@@ -562,9 +567,8 @@ __device__ __forceinline__ void dp_swar_body ( const DPArgs & a, const SwarConst
 #pragma unroll 1
                     for ( int rr = 0; rr < UR; ++rr )
                     {
-                        const uint32_t c = code_at ( cg, rr );
-                        const uint32_t * lo = s_eq + ( TAB ? c : ( c & 7u ) ) * ( W * kDPThreads ) + tid;
-                        const uint32_t * hi = s_hi + ( c >> 3 ) * ( W * kDPThreads ) + tid;
+                        const uint32_t * lo = my_eq + rl[g + rr];
+                        const uint32_t * hi = my_hi + rh[g + rr];
 #pragma unroll
                         for ( int i = 0; i < W; ++i )
                         {
@@ -583,7 +587,7 @@ __device__ __forceinline__ void dp_swar_body ( const DPArgs & a, const SwarConst
                 const bool count_here = counting && ( ( vm >> r ) & 1u );
                 if constexpr ( TAB )
                 {
-                    const uint32_t * row = s_eq + code_at ( cur, r ) * ( W * kDPThreads ) + tid;
+                    const uint32_t * row = my_eq + rl[r];
 #pragma unroll
                     for ( int i = 0; i < W; ++i )
                     {
@@ -593,9 +597,8 @@ __device__ __forceinline__ void dp_swar_body ( const DPArgs & a, const SwarConst
                 }
                 else
                 {
-                    const uint32_t c = code_at ( cur, r );
-                    const uint32_t * lo = s_eq + ( c & 7u ) * ( W * kDPThreads ) + tid;
-                    const uint32_t * hi = s_hi + ( c >> 3 ) * ( W * kDPThreads ) + tid;
+                    const uint32_t * lo = my_eq + rl[r];
+                    const uint32_t * hi = my_hi + rh[r];
 #pragma unroll
                     for ( int i = 0; i < W; ++i )
                     {

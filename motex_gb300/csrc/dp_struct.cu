@@ -306,11 +306,30 @@ __global__ void __launch_bounds__ ( kDPThreads ) k_dp_struct1_hd ( const StructA
     uint32_t prev[B];
 #pragma unroll
     for ( int b = 0; b < B; ++b ) prev[b] = __ldg ( planes + ( size_t ) b * stride + ch.warm );
+    // packed form: every thread of the CTA walks the same text positions, so
+    // the replicated windows of a block are built once into shared memory
+    // (double-buffered: one barrier per block) instead of by every thread
+    __shared__ uint32_t s_win[2][32 * B];
     for ( uint32_t kb = ch.warm; kb < ch.end; ++kb )
     {
         uint32_t cur[B];
+        const uint32_t * win = s_win[( kb - ch.warm ) & 1];
+        if constexpr ( PK )
+        {
+            uint32_t * w = s_win[( kb - ch.warm ) & 1];
+            for ( uint32_t i = threadIdx.x; i < 32u * B; i += kDPThreads )
+            {
+                const uint32_t b = i >> 5, r = i & 31u;
+                const uint32_t pw = __ldg ( planes + ( size_t ) b * stride + kb ), cw = __ldg ( planes + ( size_t ) b * stride + kb + 1 );
+                w[i] = ( __funnelshift_rc ( pw, cw, r + 1 ) >> ( 32 - L ) ) * rep3;
+            }
+            __syncthreads ();
+        }
+        else
+        {
 #pragma unroll
-        for ( int b = 0; b < B; ++b ) cur[b] = __ldg ( planes + ( size_t ) b * stride + kb + 1 );
+            for ( int b = 0; b < B; ++b ) cur[b] = __ldg ( planes + ( size_t ) b * stride + kb + 1 );
+        }
         const uint32_t vm = __ldg ( a.text.vmask + kb ), em = __ldg ( a.text.emask + kb );
         const bool counting = kb >= ch.begin;
         // hit masks built in reverse bit order (position r at bit 31-r) as
@@ -324,8 +343,7 @@ __global__ void __launch_bounds__ ( kDPThreads ) k_dp_struct1_hd ( const StructA
             {
                 uint32_t x = 0;
 #pragma unroll
-                for ( int b = 0; b < B; ++b )
-                    x |= fp[b] ^ ( ( __funnelshift_rc ( prev[b], cur[b], r + 1 ) >> ( 32 - L ) ) * rep3 );
+                for ( int b = 0; b < B; ++b ) x |= fp[b] ^ win[b * 32 + r];
                 m0 = m0 * two + ( ( __popc ( x & mA ) * one + ne0 ) >> 31 );
                 ma = ma * two + ( ( __popc ( x & mB ) * one + ne1 ) >> 31 );
                 mb = mb * two + ( ( __popc ( x & mC ) * one + ne1 ) >> 31 );
@@ -380,8 +398,9 @@ __global__ void __launch_bounds__ ( kDPThreads ) k_dp_struct1_hd ( const StructA
             R &= ~bit;
             E &= ~bit;
         }
+        if constexpr ( ! PK )
 #pragma unroll
-        for ( int b = 0; b < B; ++b ) prev[b] = cur[b];
+            for ( int b = 0; b < B; ++b ) prev[b] = cur[b];
     }
     for ( uint32_t k = 0; k < G; ++k )
     {
@@ -663,11 +682,22 @@ __global__ void __launch_bounds__ ( kDPThreads ) k_dp_struct1_swar_blk ( const S
         }
     };
 
+    // every thread walks the same text positions: the Eq-table row offset of
+    // each position of a block is computed once into shared memory
+    // (double-buffered: one barrier per block) instead of by every thread
+    __shared__ uint32_t s_row[2][32];
+    const uint32_t * my_eq = s_eq + threadIdx.x;
     for ( uint32_t kb = ch.warm; kb < ch.end; ++kb )
     {
-        uint32_t cur[B];
+        uint32_t * rows = s_row[( kb - ch.warm ) & 1];
+        if ( threadIdx.x < 32 )
+        {
+            uint32_t c = 0;
 #pragma unroll
-        for ( int b = 0; b < B; ++b ) cur[b] = __ldg ( planes + ( size_t ) b * stride + kb + 1 );
+            for ( int b = 0; b < B; ++b ) c |= ( ( __ldg ( planes + ( size_t ) b * stride + kb + 1 ) >> threadIdx.x ) & 1u ) << b;
+            rows[threadIdx.x] = c * kDPThreads;
+        }
+        __syncthreads ();
         const uint32_t vm = __ldg ( a.text.vmask + kb ), em = __ldg ( a.text.emask + kb );
         const bool counting = kb >= ch.begin;
         // hit masks built in reverse bit order (position r at bit 31-r) as
@@ -675,10 +705,7 @@ __global__ void __launch_bounds__ ( kDPThreads ) k_dp_struct1_swar_blk ( const S
         // multiply-adds (FMA pipe), the logic ops of the step fill the ALU
         uint32_t m0 = 0, ma = 0, mb = 0;
         auto step = [&] ( int r ) {
-            uint32_t c = 0;
-#pragma unroll
-            for ( int b = 0; b < B; ++b ) c |= ( ( cur[b] >> r ) & 1u ) << b;
-            const uint32_t Eq = s_eq[c * kDPThreads + threadIdx.x];
+            const uint32_t Eq = my_eq[rows[r]];
             const uint32_t Xv = Eq | Mv;
             const uint32_t s1 = ( Eq & Pv ) * C.one + Pv;
             const uint32_t Xh = ( s1 ^ Pv ) | Eq;

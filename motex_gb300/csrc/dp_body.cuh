@@ -113,13 +113,19 @@ __device__ __forceinline__ void dp_fast_body ( const DPArgs & a, uint32_t tile, 
     {
         const uint32_t topmask = l >= 32 ? 0xffffffffu : ~( ( 1u << ( 32 - l ) ) - 1u );
         const uint32_t e = a.e;
-        uint32_t prev[B], cur[B];
-#pragma unroll
-        for ( int b = 0; b < B; ++b ) prev[b] = __ldg ( planes + ( size_t ) b * stride + ch.begin );
+        // every thread of the CTA walks the same text positions: the windows
+        // of a block (32 positions x B planes) are built once into shared
+        // memory, double-buffered so that one barrier per block suffices
+        __shared__ uint32_t s_win[2][32 * B];
         for ( uint32_t k = ch.begin; k < ch.end; ++k )
         {
-#pragma unroll
-            for ( int b = 0; b < B; ++b ) cur[b] = __ldg ( planes + ( size_t ) b * stride + k + 1 );
+            uint32_t * win = s_win[( k - ch.begin ) & 1];
+            for ( uint32_t i = threadIdx.x; i < 32u * B; i += kDPThreads )
+            {
+                const uint32_t * pl = planes + ( size_t ) ( i >> 5 ) * stride;
+                win[i] = __funnelshift_rc ( __ldg ( pl + k ), __ldg ( pl + k + 1 ), ( i & 31u ) + 1 ) & topmask;
+            }
+            __syncthreads ();
             const uint32_t vm = __ldg ( a.text.vmask + k ), em = __ldg ( a.text.emask + k );
             if ( vm == 0xffffffffu && em == 0u )
             {
@@ -132,7 +138,7 @@ __device__ __forceinline__ void dp_fast_body ( const DPArgs & a, uint32_t tile, 
                         const int r = g + rr;
                         uint32_t y[B];
 #pragma unroll
-                        for ( int b = 0; b < B; ++b ) y[b] = __funnelshift_rc ( prev[b], cur[b], r + 1 ) & topmask;
+                        for ( int b = 0; b < B; ++b ) y[b] = win[b * 32 + r];
 #pragma unroll
                         for ( int i = 0; i < W; ++i )
                         {
@@ -152,7 +158,7 @@ __device__ __forceinline__ void dp_fast_body ( const DPArgs & a, uint32_t tile, 
                     {
                         uint32_t y[B];
 #pragma unroll
-                        for ( int b = 0; b < B; ++b ) y[b] = __funnelshift_rc ( prev[b], cur[b], r + 1 ) & topmask;
+                        for ( int b = 0; b < B; ++b ) y[b] = win[b * 32 + r];
 #pragma unroll
                         for ( int i = 0; i < W; ++i )
                         {
@@ -169,8 +175,6 @@ __device__ __forceinline__ void dp_fast_body ( const DPArgs & a, uint32_t tile, 
                     }
                 }
             }
-#pragma unroll
-            for ( int b = 0; b < B; ++b ) prev[b] = cur[b];
         }
     }
     else
@@ -696,9 +700,14 @@ __device__ __forceinline__ void dp_hswar_body ( const DPArgs & a, const SwarCons
         for ( int j = 0; j < NL; ++j )
             if ( __popc ( x & ( C.FM << ( j * C.S ) ) ) <= e ) cnt[i] += 1u << ( j * C.S );
     };
-    auto window = [&] ( const uint32_t ( &prev )[B], const uint32_t ( &cur )[B], int r, uint32_t ( &Y )[B] ) {
+    // the replicated windows of a block (32 positions x B planes) are the same
+    // for every thread: built once per CTA into shared memory, double-buffered
+    // so that one barrier per block suffices
+    __shared__ uint32_t s_win[2][32 * B];
+    const uint32_t * win = s_win[0];
+    auto window = [&] ( int r, uint32_t ( &Y )[B] ) {
 #pragma unroll
-        for ( int b = 0; b < B; ++b ) Y[b] = ( __funnelshift_rc ( prev[b], cur[b], r + 1 ) >> down ) * C.REP;
+        for ( int b = 0; b < B; ++b ) Y[b] = win[b * 32 + r];
     };
     auto drain = [&] () {
 #pragma unroll
@@ -725,14 +734,18 @@ __device__ __forceinline__ void dp_hswar_body ( const DPArgs & a, const SwarCons
         }
     };
 
-    uint32_t prev[B];
-#pragma unroll
-    for ( int b = 0; b < B; ++b ) prev[b] = __ldg ( planes + ( size_t ) b * stride + ch.begin );
     for ( uint32_t k = ch.begin; k < ch.end; ++k )
     {
-        uint32_t cur[B];
-#pragma unroll
-        for ( int b = 0; b < B; ++b ) cur[b] = __ldg ( planes + ( size_t ) b * stride + k + 1 );
+        {
+            uint32_t * w = s_win[( k - ch.begin ) & 1];
+            for ( uint32_t i = threadIdx.x; i < 32u * B; i += kDPThreads )
+            {
+                const uint32_t * pl = planes + ( size_t ) ( i >> 5 ) * stride;
+                w[i] = ( __funnelshift_rc ( __ldg ( pl + k ), __ldg ( pl + k + 1 ), ( i & 31u ) + 1 ) >> down ) * C.REP;
+            }
+            win = w;
+            __syncthreads ();
+        }
         const uint32_t vm = __ldg ( a.text.vmask + k ), em = __ldg ( a.text.emask + k );
         if ( vm == 0xffffffffu && em == 0u )
         {
@@ -743,7 +756,7 @@ __device__ __forceinline__ void dp_hswar_body ( const DPArgs & a, const SwarCons
                 for ( int rr = 0; rr < UR; ++rr )
                 {
                     uint32_t Y[B];
-                    window ( prev, cur, g + rr, Y );
+                    window ( g + rr, Y );
 #pragma unroll
                     for ( int i = 0; i < W; ++i ) count ( i, Y );
                 }
@@ -756,7 +769,7 @@ __device__ __forceinline__ void dp_hswar_body ( const DPArgs & a, const SwarCons
                 if ( ( vm >> r ) & 1u )
                 {
                     uint32_t Y[B];
-                    window ( prev, cur, r, Y );
+                    window ( r, Y );
 #pragma unroll
                     for ( int i = 0; i < W; ++i ) count ( i, Y );
                 }
@@ -769,8 +782,6 @@ __device__ __forceinline__ void dp_hswar_body ( const DPArgs & a, const SwarCons
             }
         }
         drain ();
-#pragma unroll
-        for ( int b = 0; b < B; ++b ) prev[b] = cur[b];
     }
     for ( int f = 0; f < NF; ++f )
     {

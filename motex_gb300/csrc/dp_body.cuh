@@ -227,19 +227,31 @@ __device__ __forceinline__ void dp_fast_body ( const DPArgs & a, uint32_t tile, 
             for ( int b = 1; b < B; ++b ) x |= wp[i][b] ^ T[b];
             step_eq ( i, ~x );
         };
-        // table row of the symbol at bit r of the plane words
-        auto eq_row = [&] ( const uint32_t ( &pw )[B], int r ) {
-            uint32_t c = 0;
-#pragma unroll
-            for ( int b = 0; b < B; ++b ) c |= ( ( pw[b] >> r ) & 1u ) << b;
-            return s_eq + c * ( W * kDPThreads ) + threadIdx.x;
-        };
-
+        // B <= 3: every thread of the CTA walks the same text positions, so the
+        // table row of each position of a block is built once into shared
+        // memory, double-buffered so that one barrier per block suffices.
+        // B = 4, 5 form the broadcast symbol-bit masks per thread (kept: the
+        // shared form raised their register count).
+        __shared__ uint32_t s_row[2][32];
+        const uint32_t * my_eq = s_eq + threadIdx.x;
         uint32_t cur[B];
         for ( uint32_t k = ch.warm; k < ch.end; ++k )
         {
+            const uint32_t * pre = s_row[( k - ch.warm ) & 1];
+            if constexpr ( TAB )
+            {
+                if ( threadIdx.x < 32 )
+                {
+                    uint32_t c = 0;
 #pragma unroll
-            for ( int b = 0; b < B; ++b ) cur[b] = __ldg ( planes + ( size_t ) b * stride + k + 1 );
+                    for ( int b = 0; b < B; ++b ) c |= ( ( __ldg ( planes + ( size_t ) b * stride + k + 1 ) >> threadIdx.x ) & 1u ) << b;
+                    s_row[( k - ch.warm ) & 1][threadIdx.x] = c * ( W * kDPThreads );
+                }
+                __syncthreads ();
+            }
+            else
+#pragma unroll
+                for ( int b = 0; b < B; ++b ) cur[b] = __ldg ( planes + ( size_t ) b * stride + k + 1 );
             const uint32_t vm = __ldg ( a.text.vmask + k ), em = __ldg ( a.text.emask + k );
             const bool counting = k >= ch.begin;
             if ( counting && vm == 0xffffffffu && em == 0u )
@@ -249,13 +261,13 @@ __device__ __forceinline__ void dp_fast_body ( const DPArgs & a, uint32_t tile, 
                 {
                     uint32_t cg[B];
 #pragma unroll
-                    for ( int b = 0; b < B; ++b ) cg[b] = cur[b] >> g;
+                    for ( int b = 0; b < B; ++b ) cg[b] = TAB ? 0u : cur[b] >> g;
 #pragma unroll
                     for ( int rr = 0; rr < UR; ++rr )
                     {
                         if constexpr ( TAB )
                         {
-                            const uint32_t * row = eq_row ( cg, rr );
+                            const uint32_t * row = my_eq + pre[g + rr];
 #pragma unroll
                             for ( int i = 0; i < W; ++i )
                             {
@@ -285,7 +297,7 @@ __device__ __forceinline__ void dp_fast_body ( const DPArgs & a, uint32_t tile, 
                     const bool count_here = counting && ( ( vm >> r ) & 1u );
                     if constexpr ( TAB )
                     {
-                        const uint32_t * row = eq_row ( cur, r );
+                        const uint32_t * row = my_eq + pre[r];
 #pragma unroll
                         for ( int i = 0; i < W; ++i )
                         {

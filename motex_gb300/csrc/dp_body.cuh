@@ -227,27 +227,26 @@ __device__ __forceinline__ void dp_fast_body ( const DPArgs & a, uint32_t tile, 
             for ( int b = 1; b < B; ++b ) x |= wp[i][b] ^ T[b];
             step_eq ( i, ~x );
         };
-        // B <= 3: every thread of the CTA walks the same text positions, so the
-        // table row of each position of a block is built once into shared
-        // memory, double-buffered so that one barrier per block suffices.
-        // B = 4, 5 form the broadcast symbol-bit masks per thread (kept: the
-        // shared form raised their register count).
-        __shared__ uint32_t s_row[2][32];
+        // B <= 3: every thread walks the same text positions, so each warp
+        // builds the table row of each position of a block once (lane r takes
+        // position r) into its own shared buffer, double-buffered so that one
+        // warp barrier per block suffices.  B = 4, 5 form the broadcast
+        // symbol-bit masks per thread (kept: the shared form raised their
+        // register count).
+        __shared__ uint32_t s_row[kDPThreads / 32][2][32];
+        const uint32_t lane = threadIdx.x & 31u, wid = threadIdx.x >> 5;
         const uint32_t * my_eq = s_eq + threadIdx.x;
         uint32_t cur[B];
         for ( uint32_t k = ch.warm; k < ch.end; ++k )
         {
-            const uint32_t * pre = s_row[( k - ch.warm ) & 1];
+            const uint32_t * pre = s_row[wid][( k - ch.warm ) & 1];
             if constexpr ( TAB )
             {
-                if ( threadIdx.x < 32 )
-                {
-                    uint32_t c = 0;
+                uint32_t c = 0;
 #pragma unroll
-                    for ( int b = 0; b < B; ++b ) c |= ( ( __ldg ( planes + ( size_t ) b * stride + k + 1 ) >> threadIdx.x ) & 1u ) << b;
-                    s_row[( k - ch.warm ) & 1][threadIdx.x] = c * ( W * kDPThreads );
-                }
-                __syncthreads ();
+                for ( int b = 0; b < B; ++b ) c |= ( ( __ldg ( planes + ( size_t ) b * stride + k + 1 ) >> lane ) & 1u ) << b;
+                s_row[wid][( k - ch.warm ) & 1][lane] = c * ( W * kDPThreads );
+                __syncwarp ();
             }
             else
 #pragma unroll
@@ -483,12 +482,14 @@ __device__ __forceinline__ void dp_swar_body ( const DPArgs & a, const SwarConst
         Pv[i] = Mh2 | ~( Xv | Ph2 );
         Mv[i] = Ph2 & Xv & C.NG;
     };
-    // Eq-table rows of the text positions of a block: every thread of the CTA
-    // walks the same positions, so the rows (code * W * kDPThreads; for
-    // B = 4, 5 those of the low three code bits and of the high bits) are
-    // computed once per block into shared memory, double-buffered so that one
-    // barrier per block suffices, instead of from the bit planes by every thread
-    __shared__ uint32_t s_rl[2][32], s_rh[2][32];
+    // Eq-table rows of the text positions of a block: every thread walks the
+    // same positions, so each warp computes the rows (code * W * kDPThreads;
+    // for B = 4, 5 those of the low three code bits and of the high bits) once
+    // per block, lane r taking position r, into its own shared buffer,
+    // double-buffered so that one warp barrier per block suffices, instead of
+    // every thread deriving every row from the bit planes
+    __shared__ uint32_t s_rl[kDPThreads / 32][2][32], s_rh[kDPThreads / 32][2][32];
+    const uint32_t lane = tid & 31, wid = tid >> 5;
     const uint32_t * my_eq = s_eq + tid;
     const uint32_t * my_hi = s_hi + tid;
     auto count = [&] ( int i ) { cnt[i] = ( ( ~sc[i] & C.HB ) >> sh ) * C.ONE + cnt[i]; };
@@ -519,17 +520,16 @@ __device__ __forceinline__ void dp_swar_body ( const DPArgs & a, const SwarConst
 
     for ( uint32_t k = ch.warm; k < ch.end; ++k )
     {
-        uint32_t * rl = s_rl[( k - ch.warm ) & 1];
-        uint32_t * rh = s_rh[( k - ch.warm ) & 1];
-        if ( tid < 32 )
+        uint32_t * rl = s_rl[wid][( k - ch.warm ) & 1];
+        uint32_t * rh = s_rh[wid][( k - ch.warm ) & 1];
         {
             uint32_t c = 0;
 #pragma unroll
-            for ( int b = 0; b < B; ++b ) c |= ( ( __ldg ( planes + ( size_t ) b * stride + k + 1 ) >> tid ) & 1u ) << b;
-            rl[tid] = ( TAB ? c : ( c & 7u ) ) * ( W * kDPThreads );
-            rh[tid] = ( c >> 3 ) * ( W * kDPThreads );
+            for ( int b = 0; b < B; ++b ) c |= ( ( __ldg ( planes + ( size_t ) b * stride + k + 1 ) >> lane ) & 1u ) << b;
+            rl[lane] = ( TAB ? c : ( c & 7u ) ) * ( W * kDPThreads );
+            rh[lane] = ( c >> 3 ) * ( W * kDPThreads );
         }
-        __syncthreads ();
+        __syncwarp ();
         const uint32_t vm = __ldg ( a.text.vmask + k ), em = __ldg ( a.text.emask + k );
         const bool counting = k >= ch.begin;
         if ( counting && vm == 0xffffffffu && em == 0u )

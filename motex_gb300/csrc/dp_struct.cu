@@ -682,22 +682,22 @@ __global__ void __launch_bounds__ ( kDPThreads ) k_dp_struct1_swar_blk ( const S
         }
     };
 
-    // every thread walks the same text positions: the Eq-table row offset of
-    // each position of a block is computed once into shared memory
-    // (double-buffered: one barrier per block) instead of by every thread
-    __shared__ uint32_t s_row[2][32];
+    // every thread walks the same text positions: each warp computes the
+    // Eq-table row offset of each position of a block once (lane r takes
+    // position r) into its own shared buffer (double-buffered: one warp
+    // barrier per block) instead of every thread computing all of them
+    __shared__ uint32_t s_row[kDPThreads / 32][2][32];
     const uint32_t * my_eq = s_eq + threadIdx.x;
     for ( uint32_t kb = ch.warm; kb < ch.end; ++kb )
     {
-        uint32_t * rows = s_row[( kb - ch.warm ) & 1];
-        if ( threadIdx.x < 32 )
+        uint32_t * rows = s_row[warp][( kb - ch.warm ) & 1];
         {
             uint32_t c = 0;
 #pragma unroll
-            for ( int b = 0; b < B; ++b ) c |= ( ( __ldg ( planes + ( size_t ) b * stride + kb + 1 ) >> threadIdx.x ) & 1u ) << b;
-            rows[threadIdx.x] = c * kDPThreads;
+            for ( int b = 0; b < B; ++b ) c |= ( ( __ldg ( planes + ( size_t ) b * stride + kb + 1 ) >> lane ) & 1u ) << b;
+            rows[lane] = c * kDPThreads;
         }
-        __syncthreads ();
+        __syncwarp ();
         const uint32_t vm = __ldg ( a.text.vmask + kb ), em = __ldg ( a.text.emask + kb );
         const bool counting = kb >= ch.begin;
         // hit masks built in reverse bit order (position r at bit 31-r) as

@@ -105,9 +105,14 @@ def cpu_run(binary, wl, seqs, threads, timeout=600):
             raise RuntimeError(f"{binary} failed: {p.stderr[-500:]}")
         m = re.search(r"# Run on \d+ proc\(s\) in ([0-9.]+) secs", open(out).read())
         secs = float(m.group(1))
+    return ref_cells(wl, seqs), secs
+
+
+def ref_cells(wl, seqs):
+    """Reference DP cells of an all-pairs run: sequences shorter than the motif are skipped."""
     tml = wl.k + sum(g[0] + g[2] for g in wl.boxes)
     searched = sum(len(s) for s in seqs if len(s) >= tml)
-    return searched * searched * (len(wl.boxes) + 1), secs
+    return searched * searched * (len(wl.boxes) + 1)
 
 
 def take_symbols(seqs, total):
@@ -460,7 +465,7 @@ def run_gpu(args, rank, world, local_rank):
     return out, wl
 
 
-def run_reference(args):
+def run_reference(args, world):
     """Reference arm: the CPU implementation of the path, all host threads."""
     wl = WORKLOADS[args.workload](args.scale)
     binary, kind = cpu_binary()
@@ -477,10 +482,13 @@ def run_reference(args):
     desc = sample_desc
     return {
         "impl": "reference", "metric": "GCUPS (reference DP cell updates per second), whole-set word-based motif extraction",
-        "value": round(val, 3), "unit": "GCUPS", "n_gpus": 0, "steps": args.steps, "warmup": args.warmup,
+        "value": round(val, 3), "unit": "GCUPS", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": round(secs_t * 1e3 / args.steps, 3), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "integer", "data": "synthetic (seeded generator)",
-        "config": {"workload": args.workload, "alphabet": wl.alphabet, "d": wl.d, "k": wl.k, "e": wl.e, "q": wl.q},
+        "config": {"workload": args.workload, "scale": args.scale, "alphabet": wl.alphabet, "num_seqs": len(wl.seqs),
+                   "total_len": sum(len(s) for s in wl.seqs), "d": wl.d, "k": wl.k, "e": wl.e, "q": wl.q,
+                   "ref_cells": ref_cells(wl, wl.seqs), "parallelism": f"replicas{world}",
+                   "host_threads": threads},
         "cpu_baseline": {"value": round(val, 3), "unit": "GCUPS", "cores": threads, "kind": kind, "sample": desc},
         "e2e": {"value": round(val, 3), "unit": "GCUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -508,7 +516,7 @@ def main():
 
     if args.impl == "reference":
         if rank == 0:
-            print(json.dumps(run_reference(args)), flush=True)
+            print(json.dumps(run_reference(args, world)), flush=True)
         return
 
     if world > 1:

@@ -30,3 +30,20 @@ def test_sample_takes_whole_set_when_cheap(monkeypatch):
     wl = W.Workload("small", "DNA", ["ACGTACGTAC"] * 5, d=0, k=4, e=0, q=50)
     sample, desc = bench.cpu_sample("x", wl, 8)
     assert sample == wl.seqs
+
+
+def test_reference_arm_line(monkeypatch):
+    """The reference arm reports the same config keys as the GPU arm, n_gpus as
+    launched, and its e2e as its own value (no host-device copies)."""
+    import argparse
+    monkeypatch.setattr(bench, "cpu_binary", lambda: ("x", "port"))
+    monkeypatch.setattr(bench, "cpu_run", lambda b, wl, seqs, t, timeout=600: (bench.ref_cells(wl, seqs), 0.5))
+    args = argparse.Namespace(workload="dna_hd_small", scale=1.0, steps=2, warmup=1)
+    line = bench.run_reference(args, 2)
+    assert line["impl"] == "reference" and line["n_gpus"] == 2
+    cfg = line["config"]
+    for key in ("workload", "scale", "alphabet", "num_seqs", "total_len", "d", "k", "e", "q", "ref_cells", "parallelism"):
+        assert key in cfg, key
+    assert cfg["ref_cells"] == 32000 * 32000                 # 64 x 500 nt, every sequence searched
+    assert line["e2e"]["value"] == line["value"] == line["cpu_baseline"]["value"]
+    assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["e2e"]["d2h_bytes_per_step"] == 0

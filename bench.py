@@ -57,6 +57,8 @@ WORKLOADS = {
     "dna_long": lambda s: W.dna_long(scale=s),
     "structured_d1": lambda s: W.structured(scale=s, d=1),
     "structured_d0": lambda s: W.structured(scale=s, d=0),
+    "structured2_d0": lambda s: W.structured2(scale=s, d=0),
+    "structured2_d1": lambda s: W.structured2(scale=s, d=1),
     "dna_satellite": lambda s: W.dna_satellite(scale=s),
 }
 DEFAULT_WORKLOAD = "dna_ed"
@@ -246,7 +248,9 @@ def dp_kernel_name(wl):
     """The engine's default DP kernel for the workload (bit planes B from the
     symbols present; the autotuner may pick another shape of the same kernel)."""
     if wl.boxes:
-        return "k_dp_struct1"
+        if len(wl.boxes) > 1:
+            return "k_dp_structN"
+        return "k_dp_struct1_swar_blk" if wl.d == 1 else "k_dp_struct1_hd"
     if wl.k > 32:
         return "k_dp_generic"
     sigma = len(set("".join(wl.seqs)))

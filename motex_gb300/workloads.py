@@ -21,6 +21,8 @@ Workloads (sizes as run by ``bench.py`` and the tests):
   ``-d 0 -k 20 -e 3 -q 50``.
 * ``structured``     boxes ``1 / 5 15 10 1`` with ``-k 8 -e 1`` on dna_ed's
   input.
+* ``structured2``    two gaps (``2 / 16 17 6 1 / 15 16 7 2``) with ``-k 8 -e 1``
+  on dna_ed's input.
 * ``serve_stream``   extraction requests with Poisson arrivals.
 
 ``scale`` shrinks a workload (fewer / shorter sequences) for parity tests
@@ -203,6 +205,17 @@ def structured(seed: int = 2, scale: float = 1.0, d: int = 1) -> Workload:
     w.name = "structured"
     w.k, w.e = 8, 1
     w.boxes = ((5, 15, 10, 1),)
+    return w
+
+
+def structured2(seed: int = 2, scale: float = 1.0, d: int = 0) -> Workload:
+    """Two gaps, the shape of the reference's example boxes file (gap 16-17,
+    box 6 with 1 error; gap 15-16, box 7 with 2 errors) after a k 8 e 1 first
+    box, on dna_ed's input."""
+    w = dna_ed(seed, scale, d=d)
+    w.name = "structured2"
+    w.k, w.e = 8, 1
+    w.boxes = ((16, 17, 6, 1), (15, 16, 7, 2))
     return w
 
 

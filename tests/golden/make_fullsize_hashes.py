@@ -1,11 +1,11 @@
-"""Pin the full-size configurations to the reference itself.
+"""Pin the full-size workloads to the reference itself.
 
-For each configuration below, the seeded input is generated (the same
+For each workload below, the seeded input is generated (the same
 generators the benchmark and the GPU tests use), the reference MoTeX built by
 oracle/build_ref.sh (motexOMP, all host threads) is run on it, and the
 SHA-256 and line count of its output file -- without the two volatile header
 lines -- are stored in tests/golden/fullsize.json.  The outputs are too large
-to commit (config 2 prints 441,205 motifs); tests/test_gpu_fullsize_ref.py
+to commit (dna_ed prints 441,205 motifs); tests/test_gpu_fullsize_ref.py
 regenerates each input, runs motexGPU with the same switches and compares the
 hash.  Each reference run takes from minutes to about an hour on 8 cores;
 entries are written as they finish, and existing ones are kept unless named
@@ -35,13 +35,13 @@ REF = os.path.join(ROOT, "oracle", "_ref", "motexOMP")
 
 # name -> (workload factory, description)
 CASES = {
-    "c2_dna_ed": (lambda: W.dna_ed(), "config 2: DNA 1200 x U[800,1200], -d 1 -k 15 -e 3 -q 10"),
-    "c3_prot_d0": (lambda: W.prot_uneven(d=0), "config 3: PROT 2000 x logU[50,2000], -d 0 -k 10 -e 2 -q 15"),
-    "c3_prot_d1": (lambda: W.prot_uneven(d=1), "config 3: PROT 2000 x logU[50,2000], -d 1 -k 10 -e 2 -q 15"),
-    "c4_dna_long_tenth": (lambda: W.dna_long(scale=0.1),
-                          "config 4 at 1/10 length: DNA 8 x 100 knt with tandem repeats, -d 0 -k 20 -e 3 -q 50"),
-    "c4s_struct_d0": (lambda: W.structured(d=0), "config 4 structured on config 2's input: -k 8 -e 1 -s (5-15, 10, 1), -d 0"),
-    "c4s_struct_d1": (lambda: W.structured(d=1), "config 4 structured on config 2's input: -k 8 -e 1 -s (5-15, 10, 1), -d 1"),
+    "dna_ed": (lambda: W.dna_ed(), "dna_ed: DNA 1200 x U[800,1200], -d 1 -k 15 -e 3 -q 10"),
+    "prot_uneven_d0": (lambda: W.prot_uneven(d=0), "prot_uneven: PROT 2000 x logU[50,2000], -d 0 -k 10 -e 2 -q 15"),
+    "prot_uneven_d1": (lambda: W.prot_uneven(d=1), "prot_uneven: PROT 2000 x logU[50,2000], -d 1 -k 10 -e 2 -q 15"),
+    "dna_long_tenth": (lambda: W.dna_long(scale=0.1),
+                       "dna_long at 1/10 length: DNA 8 x 100 knt with tandem repeats, -d 0 -k 20 -e 3 -q 50"),
+    "structured_d0": (lambda: W.structured(d=0), "structured motifs on dna_ed's input: -k 8 -e 1 -s (5-15, 10, 1), -d 0"),
+    "structured_d1": (lambda: W.structured(d=1), "structured motifs on dna_ed's input: -k 8 -e 1 -s (5-15, 10, 1), -d 1"),
 }
 
 

@@ -50,6 +50,17 @@ def strip_volatile(text: str) -> str:
                    if not l.startswith(("# Rundate:", "# Run on ", "User time:")))
 
 
+def input_sha256(w) -> str:
+    """SHA-256 of a workload's input (sequences, one per line, and the boxes)."""
+    h = hashlib.sha256()
+    for seq in w.seqs:
+        h.update(seq.encode())
+        h.update(b"\n")
+    if w.boxes:
+        h.update(repr(tuple(tuple(g) for g in w.boxes)).encode())
+    return h.hexdigest()
+
+
 def run_case(name):
     w = CASES[name][0]()
     with tempfile.TemporaryDirectory() as tmp:
@@ -65,7 +76,7 @@ def run_case(name):
         secs = time.time() - t0
         with open(os.path.join(tmp, "out.motex")) as f:
             text = strip_volatile(f.read())
-    return {"args": args, "description": CASES[name][1],
+    return {"args": args, "description": CASES[name][1], "input_sha256": input_sha256(w),
             "sha256": hashlib.sha256(text.encode()).hexdigest(),
             "lines": text.count("\n"), "reference": "motexOMP", "threads": os.cpu_count(),
             "reference_seconds": round(secs, 1)}

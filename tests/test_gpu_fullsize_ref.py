@@ -35,6 +35,17 @@ def test_table_covers_the_configurations():
         assert len(e["sha256"]) == 64 and e["lines"] >= 14, name
 
 
+@pytest.mark.parametrize("name", sorted(TABLE))
+def test_inputs_match_pinned_generators(name):
+    """The seeded generators still produce the inputs the reference ran on
+    (CPU check: a changed generator would otherwise show up only as a GPU
+    hash mismatch)."""
+    entry = TABLE[name]
+    if "input_sha256" not in entry:
+        pytest.skip("entry made before inputs were hashed")
+    assert _gen.input_sha256(_gen.CASES[name][0]()) == entry["input_sha256"]
+
+
 @pytest.mark.gpu
 @pytest.mark.parametrize("name", sorted(TABLE))
 def test_fullsize_matches_reference_hash(native_built, name):

@@ -21,8 +21,9 @@ and the SMILE file's ``User time:`` line are removed from stored outputs.  Cases
 in.boxes, out.motex) from the case directory, so the header's file lines are
 reproducible.
 
-usage: python tests/golden/make_golden.py   (needs the reference tree and an
-x86-64 host; run oracle/build_ref.sh and make -C oracle first)
+usage: python tests/golden/make_golden.py [--only NAME ...]   (needs the reference
+tree and an x86-64 host; run oracle/build_ref.sh and make -C oracle first;
+--only rebuilds the named cases and keeps the others)
 """
 from __future__ import annotations
 
@@ -46,7 +47,7 @@ REF = os.path.join(ROOT, "oracle", "_ref")
 PORT = os.path.join(ROOT, "oracle", "_build", "motex_port")
 
 
-SMILE_CASES = {"c1_dna_hd_64x500", "prot_hd_20seq", "prot_ed_20seq", "usr_hd", "dna_with_N_ed",
+SMILE_CASES = {"dna_hd_64x500", "prot_hd_20seq", "prot_ed_20seq", "usr_hd", "dna_with_N_ed",
                "quorum_boundary_q29", "short_seqs_ed", "struct_planted_hd", "struct_planted_ed",
                "struct2_planted_ed", "struct_long_gap_hd"}
 
@@ -202,7 +203,7 @@ def raw_fasta_text(seed):
 def cases():
     """(name, workload, extra CLI tokens, raw FASTA text or None)"""
     out = []
-    out.append(("c1_dna_hd_64x500", W.dna_hd_small(seed=1), [], None))
+    out.append(("dna_hd_64x500", W.dna_hd_small(seed=1), [], None))
     out.append(("dna_ed_24seq", W.dna_ed(seed=2, scale=0.02), [], None))
     out.append(("dna_hd_24seq", W.dna_ed(seed=2, scale=0.02, d=0), [], None))
     out.append(("prot_hd_20seq", W.prot_uneven(seed=3, scale=0.01, d=0), [], None))
@@ -239,6 +240,14 @@ def cases():
     w = W.dna_ed(seed=21, scale=0.005, d=0)
     w.k, w.e, w.q = 7, 1, 20
     out.append(("flag_L_ignored", w, ["-L", "1"], None))
+    # 4-mers with 2-3 errors hit at nearly every position: a packed lane's hit
+    # count for a 32-position block must not carry into its neighbour
+    w = W.dna_ed(seed=24, scale=0.006, d=1)
+    w.k, w.e, w.q = 4, 3, 30
+    out.append(("short_factor_k4_e3_dna_ed", w, [], None))
+    w = W.prot_uneven(seed=25, scale=0.004, d=1)
+    w.k, w.e, w.q = 4, 2, 30
+    out.append(("short_factor_k4_e2_prot_ed", w, [], None))
     return out
 
 
@@ -330,12 +339,15 @@ def build_mode_case(name, w, bg_seqs, bg_q, extra, kind):
 
 
 def main():
+    only = set(sys.argv[sys.argv.index("--only") + 1:]) if "--only" in sys.argv else None
     if not os.path.exists(os.path.join(REF, "motexCPU")):
         sys.exit("make_golden: oracle/_ref/motexCPU missing (run oracle/build_ref.sh on x86-64)")
     if not os.path.exists(PORT):
         sys.exit("make_golden: oracle/_build/motex_port missing (run make -C oracle)")
     os.makedirs(CASES_DIR, exist_ok=True)
     for name, w, extra, raw in cases():
+        if only is not None and name not in only:
+            continue
         d = os.path.join(CASES_DIR, name)
         if os.path.isdir(d):
             shutil.rmtree(d)
@@ -373,7 +385,8 @@ def main():
         print(f"{name:28s} seqs={len(w.seqs) if raw is None else 'raw':>5} "
               f"lines={ref_out.count(chr(10)):6d} ok")
     for case in mode_cases():
-        build_mode_case(*case)
+        if only is None or case[0] in only:
+            build_mode_case(*case)
 
 
 if __name__ == "__main__":

@@ -56,7 +56,7 @@ def test_port_modes_match_reference_golden(oracle_port, name):
 
 def test_golden_set_is_complete():
     names = set(golden_cases())
-    for needed in ("c1_dna_hd_64x500", "dna_ed_24seq", "prot_hd_20seq", "prot_ed_20seq", "struct_planted_hd",
+    for needed in ("dna_hd_64x500", "dna_ed_24seq", "prot_hd_20seq", "prot_ed_20seq", "struct_planted_hd",
                    "struct_planted_ed", "quorum_boundary_q29", "dna_with_N_ed", "short_seqs_ed",
                    "long_factor_k70_ed", "q0_n0_all_words", "caps_Q60_n2_N40"):
         assert needed in names

@@ -105,3 +105,66 @@ def test_narrow_stride_overflows_for_k4():
     pats = ["".join(rng.choice("ACGT") for _ in range(l)) for _ in range(lanes(l, S))]
     text = "".join(rng.choice("ACGT") for _ in range(200))
     assert swar_counts(pats, text, l, e, S) != [sum(sellers_hits(p, text, e)) for p in pats]
+
+
+# ------------------------------------------------------- packed Hamming lanes
+
+def hswar_counts(pats, text, l, e):
+    """dp_hswar_body restated: NL factors of l bits per register (no guards),
+    the text window replicated into every lane by one multiply with
+    REP = sum 2^(j*l), a masked popc per lane, counts in l-bit fields drained
+    every 32 positions.  Symbols are compared as whole codes here (one plane);
+    the kernel ORs the XORs of its B planes, which is the same mismatch bit."""
+    NL = len(pats)
+    REP = sum(1 << (j * l) for j in range(NL))
+    FM = (1 << l) - 1
+    codes = {c: i for i, c in enumerate(sorted(set(text) | set("".join(pats))))}
+    nbits = max(1, (len(codes) - 1).bit_length())
+    planes_p = [[0] * NL for _ in range(nbits)]
+    for j, p in enumerate(pats):
+        for q, ch in enumerate(p):
+            for b in range(nbits):
+                if (codes[ch] >> b) & 1:
+                    planes_p[b][j] |= 1 << (j * l + q)
+    cnt, counts = 0, [0] * NL
+    for k in range(len(text)):
+        x = 0
+        if k >= l - 1:
+            win = text[k - l + 1:k + 1]
+            for b in range(nbits):
+                w = sum(((codes[ch] >> b) & 1) << q for q, ch in enumerate(win))
+                Y = (w * REP) & M32                       # no carries: the copies do not overlap
+                x |= sum(planes_p[b]) ^ Y
+            for j in range(NL):
+                if bin(x & (FM << (j * l))).count("1") <= e:
+                    cnt = (cnt + (1 << (j * l))) & M32
+        if k % 32 == 31 or k == len(text) - 1:
+            for j in range(NL):
+                counts[j] += (cnt >> (j * l)) & FM
+            cnt = 0
+    return counts
+
+
+def hamming_hits(p, t, e):
+    l = len(p)
+    return sum(1 for k in range(l - 1, len(t)) if sum(a != b for a, b in zip(p, t[k - l + 1:k + 1])) <= e)
+
+
+@pytest.mark.parametrize("l", range(6, 17))
+def test_packed_hamming_lanes_match(l):
+    rng = random.Random(300 + l)
+    NL = 32 // l
+    for e in (0, 1, l // 2, l - 1):
+        for alpha in ("ACG", "ACDEFGHIKLMNPQRSTVWY"):
+            pats = ["".join(rng.choice(alpha) for _ in range(l)) for _ in range(NL)]
+            text = "".join(rng.choice(alpha) for _ in range(150))
+            assert hswar_counts(pats, text, l, e) == [hamming_hits(p, text, e) for p in pats], (l, e, alpha)
+
+
+def test_packed_hamming_needs_six_bit_lanes():
+    """l = 5 fields hold 31 hits: a block of 32 hits (a repeat that matches at
+    every position) overflows; l = 6 fields hold it."""
+    text = "A" * 100
+    for l, ok in ((5, False), (6, True)):
+        pats = ["A" * l] * (32 // l)
+        assert (hswar_counts(pats, text, l, 0) == [hamming_hits(p, text, 0) for p in pats]) == ok, l

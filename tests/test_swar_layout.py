@@ -168,3 +168,95 @@ def test_packed_hamming_needs_six_bit_lanes():
     for l, ok in ((5, False), (6, True)):
         pats = ["A" * l] * (32 // l)
         assert (hswar_counts(pats, text, l, 0) == [hamming_hits(p, text, 0) for p in pats]) == ok, l
+
+
+# ------------------------------------- structured lanes of different lengths
+
+def struct_shape(l0, e0, b1, e1):
+    """hswar_shape (dp_struct.cu) restated: box 0 and the two box-1 rows as
+    lanes of l0, b1, b1 bits with a guard bit above each; score fields shifted
+    down from each lane's top bit by the common s = min(l0, b1) - 1; None when
+    the register or the field condition does not hold."""
+    Ls, es = (l0, b1, b1), (e0, e1, e1)
+    offs = (0, l0 + 1, l0 + b1 + 2)
+    if offs[2] + b1 > 32:
+        return None
+    s = min(l0, b1) - 1
+    if not 1 <= s <= 30:
+        return None
+    if any(e + 1 > (1 << s) or L - e - 1 >= (1 << s) for L, e in zip(Ls, es)):
+        return None
+    return offs, s
+
+
+def struct_hits(words, text, offs, s, es, check=True):
+    """Per lane, per text position: the top-bit hit test of the packed step."""
+    Ls = [len(w) for w in words]
+    HB = guards = K = SC0 = 0
+    for L, e, o in zip(Ls, es, offs):
+        hb = o + L - 1
+        HB |= 1 << hb
+        if o + L < 32:
+            guards |= 1 << (o + L)
+        K += ((1 << s) - (e + 1)) << (hb - s)
+        SC0 += L << (hb - s)
+    NG = ~guards & M32
+    NGm1 = NG & ~HB & M32
+    eq = {}
+    for c in set(text):
+        x = 0
+        for w, o in zip(words, offs):
+            for q, ch in enumerate(w):
+                if ch == c:
+                    x |= 1 << (o + q)
+        eq[c] = (x | guards) & M32
+    Pv, Mv, sc = NG, 0, (SC0 + K) & M32
+    out = [[] for _ in words]
+    for ch in text:
+        Eq = eq[ch]
+        Xv = Eq | Mv
+        s1 = ((Eq & Pv) + Pv) & M32
+        Xh = (s1 ^ Pv) | Eq
+        Ph = (Mv | ~(Xh | Pv)) & M32
+        Mhs = Pv & Xh & NGm1
+        mh = Pv & Xh & HB
+        ph = Ph & HB
+        sc = (sc + (ph >> s) - (mh >> s)) & M32
+        Ph2, Mh2 = (Ph << 1) & M32, (Mhs << 1) & M32
+        Pv = (Mh2 | ~(Xv | Ph2)) & M32
+        Mv = Ph2 & Xv & NG
+        hits = ~sc & HB
+        for i, (L, o) in enumerate(zip(Ls, offs)):
+            out[i].append(bool((hits >> (o + L - 1)) & 1))
+    return out
+
+
+def test_structured_lanes_match_sellers():
+    rng = random.Random(11)
+    done = 0
+    while done < 300:
+        l0, b1 = rng.randint(2, 14), rng.randint(2, 14)
+        e0, e1 = rng.randint(0, l0 - 1), rng.randint(0, b1 - 1)
+        shape = struct_shape(l0, e0, b1, e1)
+        if shape is None:
+            continue
+        offs, s = shape
+        alpha = rng.choice(["ACGT", "ACDEFGHIKLMNPQRSTVWY"])
+        words = ["".join(rng.choice(alpha) for _ in range(L)) for L in (l0, b1, b1)]
+        text = "".join(rng.choice(alpha) for _ in range(80))
+        got = struct_hits(words, text, offs, s, (e0, e1, e1))
+        for w, e, g in zip(words, (e0, e1, e1), got):
+            assert g == sellers_hits(w, text, e), (l0, e0, b1, e1)
+        done += 1
+
+
+def test_structured_field_condition_is_needed():
+    """l0 = 3 gives s = 2: a 12-symbol row with 1 error has l - e - 1 = 10 >= 2^s,
+    so score + 2^s - (e+1) passes 2^(s+1) while the score climbs from 0 and the
+    top-bit test reads false hits (scores 6-9)."""
+    assert struct_shape(3, 1, 12, 1) is None
+    words, es = ["AAA", "A" * 12, "A" * 12], (1, 1, 1)
+    offs, s = (0, 4, 17), 2
+    text = "A" * 12 + "C" * 20
+    got = struct_hits(words, text, offs, s, es)
+    assert any(g != sellers_hits(w, text, e) for w, e, g in zip(words, es, got))

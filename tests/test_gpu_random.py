@@ -40,6 +40,26 @@ def random_case(rng):
     return seqs, args
 
 
+DENSE_HIT_SHAPES = [("DNA", 4, 3), ("DNA", 4, 2), ("PROT", 4, 3), ("USR", 4, 3), ("DNA", 5, 4), ("PROT", 5, 3)]
+
+
+def dense_hit_case(kind, l, e):
+    """(files, args): short factors with many errors over 9 random sequences."""
+    rng = random.Random(77 + l * 10 + e)
+    letters = {"DNA": "ACGT", "PROT": W.AMINO20, "USR": "0123456789"}[kind]
+    seqs = ["".join(rng.choice(letters) for _ in range(rng.randint(60, 700))) for _ in range(9)]
+    args = ["-a", kind, "-i", "in.fa", "-o", "out.motex", "-d", "1", "-k", str(l), "-e", str(e), "-q", "30"]
+    return {"in.fa": fasta(seqs)}, args
+
+
+def long_chunk_case(d):
+    """(files, args): 8 x 6000 nt with tandem repeats, long enough that the DP
+    cuts every sequence into several text chunks."""
+    wl = W.dna_long(seed=31, scale=0.006)
+    wl.d, wl.k, wl.e, wl.q = d, 12, 2, 25
+    return {"in.fa": fasta(wl.seqs)}, wl.cli("in.fa", "out.motex")
+
+
 @pytest.mark.gpu
 @pytest.mark.parametrize("seed", range(24))
 def test_random_whole_set(native_built, oracle_port, seed):
@@ -53,17 +73,12 @@ def test_random_whole_set(native_built, oracle_port, seed):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("kind,l,e", [("DNA", 4, 3), ("DNA", 4, 2), ("PROT", 4, 3), ("USR", 4, 3),
-                                      ("DNA", 5, 4), ("PROT", 5, 3)])
+@pytest.mark.parametrize("kind,l,e", DENSE_HIT_SHAPES)
 def test_short_factors_dense_hits(native_built, oracle_port, kind, l, e):
     """Short factors with many errors hit at nearly every text position:
     the count field of each packed edit-distance lane must hold all 32 hits
     of a text block without carrying into its neighbour."""
-    rng = random.Random(77 + l * 10 + e)
-    letters = {"DNA": "ACGT", "PROT": W.AMINO20, "USR": "0123456789"}[kind]
-    seqs = ["".join(rng.choice(letters) for _ in range(rng.randint(60, 700))) for _ in range(9)]
-    args = ["-a", kind, "-i", "in.fa", "-o", "out.motex", "-d", "1", "-k", str(l), "-e", str(e), "-q", "30"]
-    files = {"in.fa": fasta(seqs)}
+    files, args = dense_hit_case(kind, l, e)
     g = run_cli(native_built.CLI_PATH, None, args, files=files)
     o = run_cli(oracle_port, None, args + ["-t", "8"], files=files)
     assert g[0] == o[0] == 0, g[2] + o[2]
@@ -76,10 +91,7 @@ def test_short_factors_dense_hits(native_built, oracle_port, kind, l, e):
 def test_long_sequences_split_across_chunks(native_built, oracle_port, d):
     """Few long sequences: the DP cuts every sequence into several text
     chunks, so presence must be counted once per sequence across chunks."""
-    wl = W.dna_long(seed=31, scale=0.006)          # 8 x 6000 nt with tandem repeats
-    wl.d, wl.k, wl.e, wl.q = d, 12, 2, 25
-    files = {"in.fa": fasta(wl.seqs)}
-    args = wl.cli("in.fa", "out.motex")
+    files, args = long_chunk_case(d)
     g = run_cli(native_built.CLI_PATH, None, args, files=files)
     o = run_cli(oracle_port, None, args + ["-t", "8"], files=files)
     assert g[0] == o[0] == 0

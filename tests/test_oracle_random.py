@@ -3,7 +3,8 @@
 libflasm.so) on the seeded random inputs of the GPU parity tests: whole sets
 (alphabets, factor lengths on both sides of the 32- and 64-symbol kernel
 boundaries, short sequences, quorum and occurrence bounds) and structured
-motifs with one and two gaps.  The GPU tests compare motexGPU with the port
+motifs with one and two gaps, short factors that hit almost everywhere, and
+long sequences cut into text chunks.  The GPU tests compare motexGPU with the port
 on exactly these inputs; this pins the port to the reference there.  The
 reference build is x86-64 only (the shipped libflasm.so), so the test is
 skipped where it is absent."""
@@ -14,7 +15,7 @@ import pytest
 
 from conftest import ORACLE_DIR
 from helpers import run_cli
-from test_gpu_random import fasta, random_case
+from test_gpu_random import DENSE_HIT_SHAPES, dense_hit_case, fasta, long_chunk_case, random_case
 from test_gpu_random_struct import boxes_text, random_struct_case
 
 REF_OMP = os.path.join(ORACLE_DIR, "_ref", "motexOMP")
@@ -43,3 +44,20 @@ def test_port_matches_reference_random_structured(oracle_port, seed):
     o = run_cli(oracle_port, None, args + ["-t", THREADS], files=files)
     assert r[0] == o[0] == 0, r[2] + o[2]
     assert r[1] == o[1]
+
+
+def _same(port, files, args):
+    r = run_cli(REF_OMP, None, args + ["-t", THREADS], files=files)
+    o = run_cli(port, None, args + ["-t", THREADS], files=files)
+    assert r[0] == o[0] == 0, r[2] + o[2]
+    assert r[1] == o[1]
+
+
+@pytest.mark.parametrize("kind,l,e", DENSE_HIT_SHAPES)
+def test_port_matches_reference_dense_hits(oracle_port, kind, l, e):
+    _same(oracle_port, *dense_hit_case(kind, l, e))
+
+
+@pytest.mark.parametrize("d", [0, 1])
+def test_port_matches_reference_long_chunks(oracle_port, d):
+    _same(oracle_port, *long_chunk_case(d))

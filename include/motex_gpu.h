@@ -252,6 +252,17 @@ const char * motex_gpu_last_error ( void );
 uint64_t motex_ctx_launches ( const motex_ctx * ctx );
 
 /*
+ * Autotuner query (no counterpart in the reference): the DP launch shape the
+ * autotuner holds for the key (bit planes B, factor length l, errors e,
+ * distance d) -- register words per thread W, factors per register NL,
+ * block unroll UR -- from tuning done in this process or read from the file
+ * MOTEX_TUNE_CACHE names (one "B l e d W NL UR" line per entry; lines naming
+ * a shape the kernels do not implement are ignored).  MOTEX_ENOTFOUND if the
+ * key has no entry.  Host-only: needs no GPU.
+ */
+int motex_tune_lookup ( int B, uint32_t l, uint32_t e, uint32_t d, int * W, int * NL, int * UR );
+
+/*
  * Measurement utility (no counterpart in the reference): sustained
  * throughput of the integer pipes on device `device`, in 10^12 operations
  * per second, from dependent-chain microkernels with enough independent
@@ -278,9 +289,14 @@ int motex_probe_int_peak ( int device, double * lop3_tops, double * iadd_tops, d
  *     larger sizes return MOTEX_EUNSUPPORTED.
  * All intermediate data lives in one 4 MiB static device array that every
  * GPU loading this library keeps until the process exits.  The first call
- * on a device resolves that array's address (with the device current), so
- * make it before any stream capture.  Calls share the array: calls that
- * overlap on the GPU race and must be serialised by the caller.
+ * on a device looks up that array's address (with the device current) and
+ * keeps it for the CUDA context it was looked up in; a call in a new context
+ * of the device (e.g. after cudaDeviceReset) looks it up again.  Make the
+ * first call on a device before any stream capture.  The call returns only
+ * after `stream` has finished its work (it reads an error word back).  A
+ * CUDA error already pending on the calling thread makes the call return
+ * MOTEX_ECUDA at once and is left pending.  Calls share the array: calls
+ * that overlap on the GPU race and must be serialised by the caller.
  */
 int motex_gpu_extract_pair_static ( const motex_params * prm, const char * alphabet,
                                     const char * d_p, uint32_t m, const char * d_t, uint32_t n,

@@ -155,7 +155,10 @@ __global__ void k_presence ( const uint8_t * __restrict__ raw, uint64_t total, u
 namespace
 {
 
-constexpr uint32_t kStageWaitLimit = 1u << 22;   // try_wait polls before a staging wait gives up
+// try_wait polls before the drain of a failed CTA gives up.  A bulk copy of
+// one tile from valid global memory lands within microseconds; each poll
+// suspends the thread for at most the hardware's try_wait window.
+constexpr uint32_t kDrainWaitPolls = 1u << 24;
 
 __device__ __forceinline__ uint32_t smem_u32 ( const void * p ) { return ( uint32_t ) __cvta_generic_to_shared ( p ); }
 
@@ -182,10 +185,11 @@ __device__ __forceinline__ bool mbar_try_wait ( uint64_t * bar, uint32_t parity 
     return done != 0;
 }
 
-// Bounded wait for the completion of phase `parity`; false if it gave up.
-__device__ __forceinline__ bool mbar_wait_bounded ( uint64_t * bar, uint32_t parity )
+// Wait of at most `polls` polls for the completion of phase `parity`;
+// false if it gave up (at once for polls = 0).
+__device__ __forceinline__ bool mbar_wait_bounded ( uint64_t * bar, uint32_t parity, uint32_t polls )
 {
-    for ( uint32_t it = 0; it < kStageWaitLimit; ++it )
+    for ( uint32_t it = 0; it < polls; ++it )
         if ( mbar_try_wait ( bar, parity ) ) return true;
     return false;
 }
@@ -212,6 +216,14 @@ __device__ __forceinline__ void bulk_copy_g2s ( void * dst, const void * src, ui
  * coalesced), and the warp forms block k0+i's bit planes, validity and end
  * masks by ballot; lane i keeps them, so every plane and mask row leaves as
  * one coalesced 128-byte store per warp.
+ *
+ * Failure path: a staging wait that gives up (a.wait_polls polls) sets bit 0
+ * of *a.err.  The CTA then issues no further copy and packs the rest of its
+ * tiles from global memory with plain loads, so every output row is written
+ * and later stages read well-formed data; the host reports the run as a
+ * timed-out device wait.  Before the CTA exits it waits (kDrainWaitPolls,
+ * bit 1 of *a.err if that gives up too) for the copies it had in flight, so
+ * none lands in shared memory the CTA no longer owns.
  */
 __global__ void __launch_bounds__ ( kPackThreads ) k_pack ( PackArgs a )
 {
@@ -240,28 +252,34 @@ __global__ void __launch_bounds__ ( kPackThreads ) k_pack ( PackArgs a )
     if ( blockIdx.x < ntiles && threadIdx.x == 0 ) issue ( blockIdx.x, 0 );
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint32_t full = 0xffffffffu;
-    bool failed = false, next_issued = false;
-    uint32_t n = 0;
+    bool failed = false, fail_next_issued = false;
+    uint32_t n = 0, n_fail = 0;
     for ( uint64_t t = blockIdx.x; t < ntiles; t += gridDim.x, ++n )
     {
         const int buf = n & 1;
-        const uint64_t tn = t + gridDim.x;
-        next_issued = tn < ntiles;
-        if ( next_issued && threadIdx.x == 0 )
+        if ( ! failed )
         {
-            // the other buffer was last read before the barrier that ended the previous tile
-            asm volatile ( "fence.proxy.async.shared::cta;" ::: "memory" );
-            issue ( tn, buf ^ 1 );
-        }
-        const bool ok = mbar_wait_bounded ( &bar[buf], ( n >> 1 ) & 1 );
-        if ( __syncthreads_or ( ! ok ) )
-        {
-            failed = true;
-            break;
+            const uint64_t tn = t + gridDim.x;
+            const bool next_issued = tn < ntiles;
+            if ( next_issued && threadIdx.x == 0 )
+            {
+                // the other buffer was last read before the barrier that ended the previous tile
+                asm volatile ( "fence.proxy.async.shared::cta;" ::: "memory" );
+                issue ( tn, buf ^ 1 );
+            }
+            const bool ok = mbar_wait_bounded ( &bar[buf], ( n >> 1 ) & 1, a.wait_polls );
+            if ( __syncthreads_or ( ! ok ) )
+            {
+                failed = true;
+                n_fail = n;
+                fail_next_issued = next_issued;
+            }
         }
 
         const uint64_t k0 = t * ( kPackTile / 32 ) + ( uint64_t ) warp * 32;     // first block of this warp
-        const uint8_t * row = stage[buf] + ( size_t ) warp * 32 * 32;
+        // staged row, or after a failed wait the same bytes from global memory
+        // (row[i * 32 + lane] is read only for positions below a.total)
+        const uint8_t * row = failed ? a.raw + k0 * 32 : stage[buf] + ( size_t ) warp * 32 * 32;
         uint64_t pos = k0 * 32 + lane;
         // sequence of this lane's first position: offs[s] <= pos < offs[s + 1]
         uint32_t s = 0;
@@ -330,10 +348,11 @@ __global__ void __launch_bounds__ ( kPackThreads ) k_pack ( PackArgs a )
     }
     if ( failed )
     {
-        if ( threadIdx.x == 0 ) atomicExch ( a.err, 1u );
         // let copies still in flight land before the CTA's shared memory goes away
-        mbar_wait_bounded ( &bar[n & 1], ( n >> 1 ) & 1 );
-        if ( next_issued ) mbar_wait_bounded ( &bar[( n + 1 ) & 1], ( ( n + 1 ) >> 1 ) & 1 );
+        bool drained = mbar_wait_bounded ( &bar[n_fail & 1], ( n_fail >> 1 ) & 1, kDrainWaitPolls );
+        if ( fail_next_issued )
+            drained &= mbar_wait_bounded ( &bar[( n_fail + 1 ) & 1], ( ( n_fail + 1 ) >> 1 ) & 1, kDrainWaitPolls );
+        if ( threadIdx.x == 0 ) atomicOr ( a.err, drained ? 1u : 3u );
     }
 }
 

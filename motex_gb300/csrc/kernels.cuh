@@ -29,8 +29,11 @@ struct PackArgs
     uint32_t *       emask;
     uint32_t *       wpos;
     uint32_t         nblk;
-    uint32_t *       err;          // set to 1 if a staging wait gave up
+    uint32_t *       err;          // bit 0: a staging wait gave up; bit 1: its drain gave up too
+    uint32_t         wait_polls;   // try_wait polls before a staging wait gives up
 };
+
+constexpr uint32_t kStageWaitPolls = 1u << 22;   // default PackArgs::wait_polls
 
 constexpr int kPackThreads = 256;              // 8 warps, each packs 32 blocks of 32 positions
 constexpr uint32_t kPackTile = 8192;           // positions (raw bytes) per staged tile

@@ -429,6 +429,24 @@ std::mutex g_tune_mu;
 std::map<TuneKey, DPTune> g_tune;
 bool g_tune_loaded = false;
 
+// A launch shape the single-motif DP kernels implement for this key: the
+// key a tunable job can have (2-5 bit planes, l <= 32, e < l, d 0/1), W 4 or
+// 8, NL 1 or the key's packed lane count, UR 4 or 8 (32 for 1-lane kernels;
+// packed Hamming only with 4).
+bool tune_entry_valid ( const TuneKey & k, const DPTune & t )
+{
+    if ( k.B < 2 || k.B > kMaxPlanes || k.l < 1 || k.l > 32 || k.e >= k.l || k.d > 1 ) return false;
+    if ( t.W != 4 && t.W != 8 ) return false;
+    const int packed = k.d == 1 ? swar_lanes ( k.l ) : ( k.B >= 3 ? hswar_lanes ( k.l ) : 1 );
+    if ( t.NL != 1 && ( t.NL != packed || packed < 2 ) ) return false;
+    if ( t.UR != 4 && t.UR != 8 && ! ( t.UR == 32 && t.NL == 1 ) ) return false;
+    if ( k.d == 0 && t.NL > 1 && t.UR != 4 ) return false;
+    return true;
+}
+
+// Entries of the MOTEX_TUNE_CACHE file, one "B l e d W NL UR" line each; a
+// line that does not parse or names a shape the kernels do not implement is
+// skipped (a later valid line for the same key wins).
 void tune_load_locked ()
 {
     if ( g_tune_loaded ) return;
@@ -437,9 +455,16 @@ void tune_load_locked ()
     if ( ! path || ! *path ) return;
     FILE * f = fopen ( path, "r" );
     if ( ! f ) return;
-    TuneKey k;
-    DPTune t;
-    while ( fscanf ( f, "%d %u %u %u %d %d %d", &k.B, &k.l, &k.e, &k.d, &t.W, &t.NL, &t.UR ) == 7 ) g_tune[k] = t;
+    char line[256];
+    while ( fgets ( line, sizeof line, f ) )
+    {
+        TuneKey k;
+        DPTune t;
+        char extra;
+        if ( sscanf ( line, "%d %u %u %u %d %d %d %c", &k.B, &k.l, &k.e, &k.d, &t.W, &t.NL, &t.UR, &extra ) != 7 )
+            continue;
+        if ( tune_entry_valid ( k, t ) ) g_tune[k] = t;
+    }
     fclose ( f );
 }
 
@@ -661,6 +686,10 @@ int stage_pack ( Job * j, bool * need_sync )
     uint32_t * scalar;
     MTX_TRY ( ensure ( j, S_SCALAR, 4, &scalar ) );
     pa.err = scalar + 3;
+    // MOTEX_PACK_WAIT_POLLS bounds the staging waits (0: give up at once, which
+    // exercises the failure path: the run returns MOTEX_ETIMEOUT)
+    pa.wait_polls = kStageWaitPolls;
+    if ( const char * w = getenv ( "MOTEX_PACK_WAIT_POLLS" ) ) pa.wait_polls = ( uint32_t ) strtoul ( w, nullptr, 10 );
     MTX_CUDA ( cudaMemsetAsync ( scalar + 3, 0, 4, st ) );
     // persistent: 8 CTAs per SM (the register and shared-memory budget allows
     // it), each with two staged tiles in flight
@@ -1127,8 +1156,9 @@ int stage_compact ( Job * j )
 int read_times ( Job * j )
 {
     MTX_CUDA ( cudaEventSynchronize ( j->ev1 ) );
-    if ( pin<uint32_t> ( j, kPinScalar )[3] )
-        return fail ( MOTEX_ECUDA, "packing: a TMA staging wait gave up (copy not completed)" );
+    if ( const uint32_t e = pin<uint32_t> ( j, kPinScalar )[3] )
+        return fail ( MOTEX_ETIMEOUT, "packing: a TMA staging wait gave up (copy not completed)%s",
+                      ( e & 2u ) ? "; so did the drain of the copies in flight" : "" );
     MTX_CUDA ( cudaEventElapsedTime ( &j->device_ms, j->ev0, j->ev1 ) );
     if ( j->dp_timed ) MTX_CUDA ( cudaEventElapsedTime ( &j->dp_ms, j->evd0, j->evd1 ) );
     return MOTEX_OK;
@@ -1748,5 +1778,17 @@ const char * motex_gpu_strerror ( int code )
 const char * motex_gpu_last_error ( void ) { return g_last_error.c_str (); }
 
 uint64_t motex_ctx_launches ( const motex_ctx * c ) { return c ? c->launches : 0; }
+
+int motex_tune_lookup ( int B, uint32_t l, uint32_t e, uint32_t d, int * W, int * NL, int * UR )
+{
+    if ( ! W || ! NL || ! UR ) return fail ( MOTEX_EINVAL, "null output pointer" );
+    DPTune t;
+    if ( ! tune_lookup ( TuneKey { B, l, e, d }, &t ) )
+        return fail ( MOTEX_ENOTFOUND, "no launch shape tuned for B=%d l=%u e=%u d=%u", B, l, e, d );
+    *W = t.W;
+    *NL = t.NL;
+    *UR = t.UR;
+    return MOTEX_OK;
+}
 
 } // extern "C"

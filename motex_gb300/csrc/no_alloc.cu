@@ -11,14 +11,23 @@
 // device array of kStaticScratchBytes, which every GPU that loads this
 // library keeps until the process exits.
 //
-// Set-up: the first call on a device (with that device current) resolves the
-// array's device address with cudaGetSymbolAddress and caches it; make that
-// first call before any stream capture.  All calls share the one array and it
-// keeps the previous call's contents, so each call clears what must start at
-// zero; calls that overlap on the GPU (different streams or host threads
-// without ordering) race on it and must be serialised by the caller.
+// Set-up: the first call on a device, with that device current, looks up the
+// array's device address with cudaGetSymbolAddress and keeps it, keyed by the
+// unique id of the CUDA context it was looked up in (cuCtxGetId; ids are never
+// reused within a process).  A later call in the same context reuses it; a
+// call in another context of the device -- e.g. the new primary context after
+// a cudaDeviceReset, which reloads the module and may move the array -- looks
+// it up again, so no call ever hands a kernel a stale address.  Make the first
+// call on a device before any stream capture.  The call returns after
+// `stream` has finished its work (it reads an error word back).  All calls
+// share the one array and it keeps the previous call's contents, so each call
+// clears what must start at zero; calls that overlap on the GPU (different
+// streams or host threads without ordering) race on it and must be
+// serialised by the caller.
 #include "motex_gpu.h"
 #include "kernels.cuh"
+
+#include <cuda.h>
 
 #include <algorithm>
 #include <mutex>
@@ -36,8 +45,14 @@ constexpr int      kMaxDevices = 64;
 
 static __device__ __align__ ( 256 ) uint8_t g_pair_scratch[kStaticScratchBytes];
 
+struct ScratchAddr
+{
+    unsigned long long ctx_id = 0;   // 0: not looked up yet (context ids start at 1)
+    uint8_t * addr = nullptr;
+};
+
 std::mutex g_mu;
-uint8_t * g_scratch_addr[kMaxDevices] = {};
+ScratchAddr g_scratch[kMaxDevices];
 
 struct AlphaMap
 {
@@ -69,18 +84,63 @@ Layout layout_for ( uint32_t B, uint32_t nblk, uint32_t U, uint32_t nchunks )
     return L;
 }
 
-// Resolve (once per device) the device address of the static scratch array.
+// The two driver calls used below, taken through the runtime's driver entry
+// point query so that the library does not link libcuda itself (hosts
+// without a driver still load it).  Called with g_mu held.
+typedef CUresult ( *PfnCtxGetCurrent ) ( CUcontext * );
+typedef CUresult ( *PfnCtxGetId ) ( CUcontext, unsigned long long * );
+PfnCtxGetCurrent g_ctx_get_current = nullptr;
+PfnCtxGetId g_ctx_get_id = nullptr;
+
+bool driver_calls ()
+{
+    if ( g_ctx_get_current && g_ctx_get_id ) return true;
+    void * a = nullptr;
+    void * b = nullptr;
+    cudaDriverEntryPointQueryResult qa, qb;
+    if ( cudaGetDriverEntryPointByVersion ( "cuCtxGetCurrent", &a, 12000, cudaEnableDefault, &qa ) != cudaSuccess ||
+         qa != cudaDriverEntryPointSuccess || ! a )
+        return false;
+    if ( cudaGetDriverEntryPointByVersion ( "cuCtxGetId", &b, 12000, cudaEnableDefault, &qb ) != cudaSuccess ||
+         qb != cudaDriverEntryPointSuccess || ! b )
+        return false;
+    g_ctx_get_current = reinterpret_cast<PfnCtxGetCurrent> ( a );
+    g_ctx_get_id = reinterpret_cast<PfnCtxGetId> ( b );
+    return true;
+}
+
+// Unique id of the calling thread's current CUDA context; 0 if none is current.
+unsigned long long current_ctx_id ()
+{
+    CUcontext c = nullptr;
+    unsigned long long id = 0;
+    if ( g_ctx_get_current ( &c ) != CUDA_SUCCESS || ! c ) return 0;
+    if ( g_ctx_get_id ( c, &id ) != CUDA_SUCCESS ) return 0;
+    return id;
+}
+
+// Device address of the static scratch array for device `dev` (current) in
+// the current context.  In host code g_pair_scratch names a host-side
+// stand-in, never a device address, so kernels only ever receive this
+// looked-up pointer.
 cudaError_t scratch_address ( int dev, uint8_t ** out )
 {
     std::lock_guard<std::mutex> lk ( g_mu );
-    if ( ! g_scratch_addr[dev] )
+    if ( ! driver_calls () ) return cudaErrorNotSupported;
+    ScratchAddr & s = g_scratch[dev];
+    const unsigned long long id = current_ctx_id ();
+    if ( id == 0 || id != s.ctx_id )
     {
         void * p = nullptr;
-        cudaError_t e = cudaGetSymbolAddress ( &p, g_pair_scratch );
+        // binds the device's primary context to this thread if none is current
+        const cudaError_t e = cudaGetSymbolAddress ( &p, g_pair_scratch );
         if ( e != cudaSuccess ) return e;
-        g_scratch_addr[dev] = static_cast<uint8_t *> ( p );
+        const unsigned long long now = current_ctx_id ();
+        if ( now == 0 ) return cudaErrorInvalidDevice;
+        s.ctx_id = now;
+        s.addr = static_cast<uint8_t *> ( p );
     }
-    *out = g_scratch_addr[dev];
+    *out = s.addr;
     return cudaSuccess;
 }
 
@@ -192,12 +252,16 @@ extern "C" int motex_gpu_extract_pair_static ( const motex_params * prm, const c
     int B = 2;                                    // the DP kernels start at two bit planes
     while ( ( 1u << B ) < sigma ) ++B;
 
+    // an error some earlier work left pending is reported and left pending,
+    // so that the launch checks below see only this call's launches
+    if ( cudaPeekAtLastError () != cudaSuccess ) return MOTEX_ECUDA;
     int dev = 0;
     if ( cudaGetDevice ( &dev ) != cudaSuccess || dev < 0 || dev >= kMaxDevices ) return MOTEX_ECUDA;
     uint8_t * base = nullptr;
     if ( scratch_address ( dev, &base ) != cudaSuccess ) return MOTEX_ECUDA;
     int sms = 0;
-    cudaDeviceGetAttribute ( &sms, cudaDevAttrMultiProcessorCount, dev );
+    if ( cudaDeviceGetAttribute ( &sms, cudaDevAttrMultiProcessorCount, dev ) != cudaSuccess || sms <= 0 )
+        return MOTEX_ECUDA;
     cudaStream_t st = static_cast<cudaStream_t> ( stream );
 
     const bool ed = prm->d == 1;

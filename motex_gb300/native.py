@@ -25,6 +25,7 @@ EXPORTS = [
     "motex_gpu_strerror", "motex_gpu_last_error", "motex_ctx_launches", "motex_probe_int_peak",
     "motex_gpu_extract_pair_static", "motex_gpu_run_batch", "motex_gpu_search",
     "motex_srv_create", "motex_srv_submit", "motex_srv_wait", "motex_srv_stats_get", "motex_srv_destroy",
+    "motex_tune_lookup",
 ]
 
 
@@ -104,6 +105,8 @@ def load_library(path: str = LIB_PATH):
         "motex_srv_destroy": (C.c_int, [C.c_void_p]),
         "motex_gpu_extract_pair_static": (C.c_int, [P(Params), C.c_char_p, C.c_void_p, C.c_uint32, C.c_void_p,
                                                     C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p]),
+        "motex_tune_lookup": (C.c_int, [C.c_int, C.c_uint32, C.c_uint32, C.c_uint32, P(C.c_int), P(C.c_int),
+                                        P(C.c_int)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -129,6 +132,17 @@ class Extraction:
     launches: int
     device_ms: float
     dp_ms: float
+
+
+def tune_lookup(B: int, l: int, e: int, d: int):
+    """(W, NL, UR) the autotuner holds for the key, or None (host-only)."""
+    lib = load_library()
+    W, NL, UR = C.c_int(), C.c_int(), C.c_int()
+    rc = lib.motex_tune_lookup(B, l, e, d, C.byref(W), C.byref(NL), C.byref(UR))
+    if rc == -7:
+        return None
+    _check(rc)
+    return W.value, NL.value, UR.value
 
 
 def probe_int_peak(device: int = 0):

@@ -42,6 +42,21 @@ CASES = {
                        "dna_long at 1/10 length: DNA 8 x 100 knt with tandem repeats, -d 0 -k 20 -e 3 -q 50"),
     "structured_d0": (lambda: W.structured(d=0), "structured motifs on dna_ed's input: -k 8 -e 1 -s (5-15, 10, 1), -d 0"),
     "structured_d1": (lambda: W.structured(d=1), "structured motifs on dna_ed's input: -k 8 -e 1 -s (5-15, 10, 1), -d 1"),
+    "structured_d1_quarter": (lambda: W.structured(d=1, scale=0.25),
+                              "structured motifs on dna_ed's input at 1/4 (300 sequences): -k 8 -e 1 -s (5-15, 10, 1), "
+                              "-d 1"),
+    "structured2_d0_quarter": (lambda: W.structured2(d=0, scale=0.25),
+                               "two-gap structured motifs on dna_ed's input at 1/4 (300 sequences): -k 8 -e 1 "
+                               "-s (16-17, 6, 1; 15-16, 7, 2), -d 0"),
+    "structured2_d1_quarter": (lambda: W.structured2(d=1, scale=0.25),
+                               "two-gap structured motifs on dna_ed's input at 1/4 (300 sequences): -k 8 -e 1 "
+                               "-s (16-17, 6, 1; 15-16, 7, 2), -d 1"),
+    "dna_long_quarter": (lambda: W.dna_long(scale=0.25),
+                         "dna_long at 1/4 length: DNA 8 x 250 knt with tandem repeats, -d 0 -k 20 -e 3 -q 50"),
+    "structured2_d0": (lambda: W.structured2(d=0),
+                       "two-gap structured motifs on dna_ed's input: -k 8 -e 1 -s (16-17, 6, 1; 15-16, 7, 2), -d 0"),
+    "structured2_d1": (lambda: W.structured2(d=1),
+                       "two-gap structured motifs on dna_ed's input: -k 8 -e 1 -s (16-17, 6, 1; 15-16, 7, 2), -d 1"),
 }
 
 

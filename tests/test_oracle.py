@@ -18,8 +18,6 @@ from conftest import ORACLE_DIR, PORT_LIB, ROOT, golden_cases, mode_cases
 from helpers import (expected_smile, load_case, load_mode_case, read_smile, run_cli, run_outputs,
                      same_but_pvalues)
 
-REFERENCE = "/root/reference"
-
 
 @pytest.mark.parametrize("name", golden_cases())
 def test_port_matches_reference_golden(oracle_port, name):
@@ -68,8 +66,10 @@ def test_golden_set_is_complete():
 
 def _difftest_binary():
     b = os.path.join(ORACLE_DIR, "_ref", "flasm_difftest")
-    if not os.path.exists(b) and os.path.isdir(REFERENCE):
-        subprocess.run([os.path.join(ORACLE_DIR, "build_ref.sh"), REFERENCE], check=True, capture_output=True)
+    if not os.path.exists(b):
+        # exit status 2: the reference sources are not on this host
+        r = subprocess.run([os.path.join(ORACLE_DIR, "build_ref.sh")], capture_output=True, text=True)
+        assert r.returncode in (0, 2), r.stdout + r.stderr
     return b
 
 

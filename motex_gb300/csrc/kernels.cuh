@@ -145,6 +145,37 @@ struct StructNArgs
     uint8_t *         split_flags;   // n_split rows of total * nstructs bytes
 };
 bool launch_dp_structN ( const StructNArgs & a, int B, bool ed, dim3 grid, cudaStream_t st );
+
+/*
+ * Block form of the any-gap structured search (dp_structn.cu).  A warp owns
+ * Pw consecutive pattern positions and, for box g+1, the Pw + D[g] - 1 rows
+ * (pattern positions P0 + lo[g] + lane) its structures reach; lane r runs
+ * one row of every box, all NR = ngaps + 1 rows packed in one register.
+ */
+constexpr uint32_t kStructNBlkMaxRows = 4;       // boxes per structure (compiled variants: 2..4)
+constexpr uint32_t kStructNBlkMaxSlots = 16;     // look-ahead ring of 32-position blocks
+struct StructNBlk
+{
+    uint32_t Pw;                                 // pattern positions per warp
+    uint32_t lo[kMaxGapsN];                      // least end offset of box g+1 over structures
+    uint32_t D[kMaxGapsN];                       // distinct end offsets of box g+1
+    uint32_t nslot;                              // ring slots: blocks E .. E + nslot - 1 are resident
+    uint32_t lo_last;                            // lo[ngaps - 1]
+    // edit distance: the rows as SWAR lanes (guard bit above each) with
+    // score fields s bits below each lane's top bit
+    uint32_t HB, NG, NGm1, K, SC0, s;
+    uint32_t off[kStructNBlkMaxRows];            // bit offset of row b's lane
+    uint32_t nm[kStructNBlkMaxRows];             // -(2^(31 - top bit of row b)): hit bit by a multiply-add
+    // Hamming: the rows as lanes of Lmax bits, factors at the top of their lanes
+    uint32_t Lmax, rep;
+    uint32_t hmask[kStructNBlkMaxRows];
+    uint32_t ne[kStructNBlkMaxRows];             // -(e_b + 1)
+    uint32_t one, two, neg1;                     // multipliers (runtime values: FMA-pipe multiply-adds)
+};
+// Fills *C and returns true when the shape has a block kernel (rows packable
+// into one register, D <= 17, look-ahead within the ring, <= 32 structures).
+bool structN_blk_shape ( const StructNArgs & a, const uint32_t * h_xoff, bool ed, StructNBlk * C );
+bool launch_dp_structN_blk ( const StructNArgs & a, const StructNBlk & C, int B, bool ed, dim3 grid, cudaStream_t st );
 __global__ void k_seq_start ( const uint32_t * offs, uint32_t nseq, uint64_t total, uint32_t * out );
 __global__ void k_wplanes_all ( const uint8_t * codes, uint32_t total, uint32_t l, uint32_t B, int top_aligned,
                                 uint32_t * out );

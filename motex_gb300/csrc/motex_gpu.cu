@@ -130,7 +130,9 @@ struct Job
     DPArgs da {};
     StructArgs sa {};
     StructNArgs san {};
+    StructNBlk snb {};
     bool structN = false;
+    bool structN_blk = false;                  // block form of the any-gap kernel
     std::vector<ChunkInfo> chunks;
     uint32_t ntiles = 0;
     uint32_t * uniq = nullptr;
@@ -965,41 +967,8 @@ int plan_structured_n ( Job * j )
         }
     }
     MTX_CUDA ( cudaMemcpyAsync ( xoff, h_xoff, ( size_t ) NS * NG * 4, cudaMemcpyHostToDevice, st ) );
-    const uint32_t ctas_x = ( T + kDPThreads - 1 ) / kDPThreads;
-    j->ntiles = ctas_x;
-    const uint32_t first_blk = j->npat ? ( j->offs[j->npat] / 32 ) : 0;
-    const uint32_t warmup = ed ? P.l + P.e - 1 : 0;
-    uint32_t nchunks = std::max<uint32_t> ( 1, ( ( uint32_t ) j->ctx->num_sms * 24 + ctas_x - 1 ) / ctas_x );
-    nchunks = std::min<uint32_t> ( nchunks, std::max<uint32_t> ( 1, ( j->nblk - first_blk ) / 16 ) );
-    build_chunks ( j, first_blk, nchunks, warmup, j->chunks );
-    ChunkInfo * d_chunks;
-    MTX_TRY ( upload_chunks ( j, &d_chunks ) );
-    uint64_t scanned = 0;
-    for ( auto & ch : j->chunks ) scanned += ( uint64_t ) ( ch.end - ch.warm ) * 32;
-    j->exec_cells = ( uint64_t ) T * scanned * ( NG + 1 );
-    const uint64_t n = ( uint64_t ) T * NS;
-    if ( n >= 0xffffff00ull ) return fail ( MOTEX_EUNSUPPORTED, "positions x gap structures exceeds 2^32" );
-    uint32_t *u_acc, *v_acc;
-    uint8_t * flags;
-    MTX_TRY ( ensure ( j, S_UACC, n, &u_acc ) );
-    MTX_TRY ( ensure ( j, S_VACC, n, &v_acc ) );
-    MTX_TRY ( ensure ( j, S_FLAGS, std::max<uint64_t> ( 1, j->n_split ) * n, &flags ) );
-    MTX_CUDA ( cudaMemsetAsync ( u_acc, 0, n * 4, st ) );
-    MTX_CUDA ( cudaMemsetAsync ( v_acc, 0, n * 4, st ) );
-    if ( j->n_split ) MTX_CUDA ( cudaMemsetAsync ( flags, 0, ( size_t ) j->n_split * n, st ) );
     StructNArgs & sa = j->san;
     sa = StructNArgs {};
-    sa.text.planes = dptr<uint32_t> ( j, S_PLANES );
-    sa.text.plane_stride = j->stride;
-    sa.text.vmask = dptr<uint32_t> ( j, S_VMASK );
-    sa.text.emask = dptr<uint32_t> ( j, S_EMASK );
-    sa.text.nblk = j->nblk;
-    sa.wpl = wpl;
-    sa.row_ok = row_ok;
-    sa.row_end = row_end;
-    sa.seq_start = seq_start;
-    sa.xoff = xoff;
-    sa.total = T;
     sa.l0 = P.l;
     sa.e0 = P.e;
     sa.blen[0] = P.l;
@@ -1011,6 +980,47 @@ int plan_structured_n ( Job * j )
     }
     sa.ngaps = NG;
     sa.nstructs = NS;
+    // block form where the shape allows: a warp owns Pw pattern positions
+    j->structN_blk = structN_blk_shape ( sa, h_xoff, ed, &j->snb );
+    const uint32_t per_cta = j->structN_blk ? ( kDPThreads / 32 ) * j->snb.Pw : kDPThreads;
+    const uint32_t ctas_x = ( T + per_cta - 1 ) / per_cta;
+    j->ntiles = ctas_x;
+    const uint32_t first_blk = j->npat ? ( j->offs[j->npat] / 32 ) : 0;
+    // edit distance restarts every box row's column this far before its
+    // first counted position (exact for the <= e test of each box)
+    uint32_t warmup = 0;
+    if ( ed )
+        for ( uint32_t b = 0; b <= NG; ++b ) warmup = std::max ( warmup, sa.blen[b] + sa.berr[b] - 1 );
+    uint32_t nchunks = std::max<uint32_t> ( 1, ( ( uint32_t ) j->ctx->num_sms * 24 + ctas_x - 1 ) / ctas_x );
+    nchunks = std::min<uint32_t> ( nchunks, std::max<uint32_t> ( 1, ( j->nblk - first_blk ) / 16 ) );
+    build_chunks ( j, first_blk, nchunks, warmup, j->chunks );
+    ChunkInfo * d_chunks;
+    MTX_TRY ( upload_chunks ( j, &d_chunks ) );
+    uint64_t scanned = 0;
+    for ( auto & ch : j->chunks ) scanned += ( uint64_t ) ( ch.end - ch.warm ) * 32;
+    // block form: every lane of a CTA runs ngaps + 1 rows
+    j->exec_cells = ( j->structN_blk ? ( uint64_t ) ctas_x * kDPThreads : ( uint64_t ) T ) * scanned * ( NG + 1 );
+    const uint64_t n = ( uint64_t ) T * NS;
+    if ( n >= 0xffffff00ull ) return fail ( MOTEX_EUNSUPPORTED, "positions x gap structures exceeds 2^32" );
+    uint32_t *u_acc, *v_acc;
+    uint8_t * flags;
+    MTX_TRY ( ensure ( j, S_UACC, n, &u_acc ) );
+    MTX_TRY ( ensure ( j, S_VACC, n, &v_acc ) );
+    MTX_TRY ( ensure ( j, S_FLAGS, std::max<uint64_t> ( 1, j->n_split ) * n, &flags ) );
+    MTX_CUDA ( cudaMemsetAsync ( u_acc, 0, n * 4, st ) );
+    MTX_CUDA ( cudaMemsetAsync ( v_acc, 0, n * 4, st ) );
+    if ( j->n_split ) MTX_CUDA ( cudaMemsetAsync ( flags, 0, ( size_t ) j->n_split * n, st ) );
+    sa.text.planes = dptr<uint32_t> ( j, S_PLANES );
+    sa.text.plane_stride = j->stride;
+    sa.text.vmask = dptr<uint32_t> ( j, S_VMASK );
+    sa.text.emask = dptr<uint32_t> ( j, S_EMASK );
+    sa.text.nblk = j->nblk;
+    sa.wpl = wpl;
+    sa.row_ok = row_ok;
+    sa.row_end = row_end;
+    sa.seq_start = seq_start;
+    sa.xoff = xoff;
+    sa.total = T;
     sa.chunks = d_chunks;
     sa.u_acc = u_acc;
     sa.v_acc = v_acc;
@@ -1028,7 +1038,9 @@ int stage_dp ( Job * j )
     const bool ed = j->prm.d == 1;
     MTX_TRY ( record ( j, j->evd0 ) );
     bool ok;
-    if ( j->structured && j->structN )
+    if ( j->structured && j->structN && j->structN_blk )
+        ok = launch_dp_structN_blk ( j->san, j->snb, j->B, ed, dim3 ( j->ntiles, ( unsigned ) j->chunks.size () ), st );
+    else if ( j->structured && j->structN )
         ok = launch_dp_structN ( j->san, j->B, ed, dim3 ( j->ntiles, ( unsigned ) j->chunks.size () ), st );
     else if ( j->structured )
         ok = launch_dp_struct1 ( j->sa, j->B, ed, dim3 ( j->ntiles, ( unsigned ) j->chunks.size () ), st );

@@ -33,6 +33,12 @@ from motex_gb300 import workloads as W  # noqa: E402
 OUT = os.path.join(HERE, "fullsize.json")
 REF = os.path.join(ROOT, "oracle", "_ref", "motexOMP")
 
+def _q(w, q):
+    """The workload with quorum q percent instead of its own."""
+    w.q = q
+    return w
+
+
 # name -> (workload factory, description)
 CASES = {
     "dna_ed": (lambda: W.dna_ed(), "dna_ed: DNA 1200 x U[800,1200], -d 1 -k 15 -e 3 -q 10"),
@@ -53,6 +59,18 @@ CASES = {
                                "-s (16-17, 6, 1; 15-16, 7, 2), -d 1"),
     "dna_long_quarter": (lambda: W.dna_long(scale=0.25),
                          "dna_long at 1/4 length: DNA 8 x 250 knt with tandem repeats, -d 0 -k 20 -e 3 -q 50"),
+    "structured_d0_quarter_q1": (lambda: _q(W.structured(d=0, scale=0.25), 1),
+                                 "structured motifs on dna_ed's input at 1/4 (300 sequences), quorum 1% so that "
+                                 "motifs print: -k 8 -e 1 -q 1 -s (5-15, 10, 1), -d 0"),
+    "structured_d1_quarter_q1": (lambda: _q(W.structured(d=1, scale=0.25), 1),
+                                 "structured motifs on dna_ed's input at 1/4 (300 sequences), quorum 1% so that "
+                                 "motifs print: -k 8 -e 1 -q 1 -s (5-15, 10, 1), -d 1"),
+    "structured2_d0_quarter_q1": (lambda: _q(W.structured2(d=0, scale=0.25), 1),
+                                  "two-gap structured motifs on dna_ed's input at 1/4 (300 sequences), quorum 1%: "
+                                  "-k 8 -e 1 -q 1 -s (16-17, 6, 1; 15-16, 7, 2), -d 0"),
+    "structured2_d1_quarter_q1": (lambda: _q(W.structured2(d=1, scale=0.25), 1),
+                                  "two-gap structured motifs on dna_ed's input at 1/4 (300 sequences), quorum 1%: "
+                                  "-k 8 -e 1 -q 1 -s (16-17, 6, 1; 15-16, 7, 2), -d 1"),
     "structured2_d0": (lambda: W.structured2(d=0),
                        "two-gap structured motifs on dna_ed's input: -k 8 -e 1 -s (16-17, 6, 1; 15-16, 7, 2), -d 0"),
     "structured2_d1": (lambda: W.structured2(d=1),
@@ -108,9 +126,13 @@ def main():
     for name in a.only or list(CASES):
         if name in table and not a.redo:
             continue
-        table[name] = run_case(name)
-        with open(OUT, "w") as f:
+        entry = run_case(name)
+        # re-read before writing: several runs may fill the table side by side
+        table = json.load(open(OUT)) if os.path.exists(OUT) else {}
+        table[name] = entry
+        with open(OUT + ".tmp", "w") as f:
             json.dump(table, f, indent=1, sort_keys=True)
+        os.replace(OUT + ".tmp", OUT)
         print(name, table[name]["lines"], table[name]["reference_seconds"], "s", flush=True)
 
 

@@ -23,10 +23,12 @@ first-occurrence compaction) of the workload.
 --impl reference times that CPU implementation alone (the reference's own
 libFLASM build is x86-64 only and its sources are not on the GPU host).
 
-Extra sections of the default line: batched_vs_plain (uneven protein batch,
-whole set in one persistent launch vs one extraction per ordered pair) and
-serving (Poisson request stream through the continuous-batching server vs
-the same arrivals served one request at a time: p50/p99 latency, throughput).
+Extra sections of the default line: batched_vs_plain (uneven protein batch:
+the whole set in one persistent launch vs the same job's static launch; the
+set cut into uneven jobs, one batch call vs one motex_gpu_run per job; and
+the per-pair drop-in) and serving (Poisson request stream through the
+continuous-batching server vs the same arrivals served one request at a
+time: p50/p99 latency, throughput).
 
 usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--workload NAME] [--impl reference]
 """
@@ -66,6 +68,7 @@ DEFAULT_WORKLOAD = "dna_ed"
 OPS_PER_CELL = {0: 6, 1: 17}
 PORT = os.path.join(ROOT, "oracle", "_build", "motex_port")
 REF_OMP = os.path.join(ROOT, "oracle", "_ref", "motexOMP")
+REF_OMP_PORT = os.path.join(ROOT, "oracle", "_ref", "motexOMP_port")
 CPU_SAMPLE_SECONDS = 12.0
 
 
@@ -81,13 +84,21 @@ def ensure_port():
 
 
 def cpu_binary():
-    """(path, kind): the reference build when it exists on this host, else the port."""
-    if os.path.exists(REF_OMP) and os.access(REF_OMP, os.X_OK):
-        try:
-            subprocess.run([REF_OMP, "-h"], capture_output=True, timeout=10)
-            return REF_OMP, "reference"
-        except OSError:
-            pass
+    """(path, kind): the CPU implementation the baselines time, the first that
+    runs on this host of
+      oracle/_ref/motexOMP       the reference built from its sources, linked to
+                                 its shipped libflasm.so (x86-64 only);
+      oracle/_ref/motexOMP_port  the reference's own driver and writers (its
+                                 unmodified sources) over the restated flasm;
+      oracle/_build/motex_port   the CPU restatement of the whole path.
+    The first two exist where the reference sources are (oracle/build_ref.sh)."""
+    for binary, kind in ((REF_OMP, "reference"), (REF_OMP_PORT, "reference (restated flasm)")):
+        if os.path.exists(binary) and os.access(binary, os.X_OK):
+            try:
+                subprocess.run([binary, "-h"], capture_output=True, timeout=10)
+                return binary, kind
+            except OSError:
+                pass
     ensure_port()
     return PORT, "port"
 
@@ -263,32 +274,81 @@ def dp_kernel_name(wl):
 
 
 def batched_vs_plain(native, ctx, seed=3, sample=30, scale=1.0):
-    """Uneven protein batch (-d 1 -k 10 -e 2 -q 15): the batched persistent
-    form on the whole set against the plain per-pair path (one extraction
-    launch sequence per ordered pair, the reference driver's loop) timed on
-    the ordered pairs of a sample of the sequences."""
+    """Uneven protein batch (-d 1 -k 10 -e 2 -q 15), batched against plain
+    three ways:
+
+    * whole: the whole set as one job through motex_gpu_run_batch (the DP as
+      one persistent launch fed from the device work queue) against the same
+      job through motex_gpu_run (one static-grid DP launch); DP device time
+      (CUDA events) and host wall time of each;
+    * jobs: the set cut into uneven jobs of 5-40 consecutive sequences, one
+      motex_gpu_run_batch call against the same jobs run one after another
+      through motex_gpu_run (host wall time, results compared);
+    * per_pair: the per-pair drop-in (motex_gpu_extract_pair, one extraction
+      launch sequence per ordered pair, the reference driver's loop) on the
+      ordered pairs of the first `sample` sequences (host wall time)."""
+    import random as _r
     import time as _t
     wl = W.prot_uneven(seed=seed, d=1, scale=scale)
     prm = native.make_params(wl.d, wl.k, wl.e, wl.q)
+    out = {"workload": "prot_uneven_d1"}
+
+    def best(fn, reps=3):
+        r, t = None, 1e30
+        for _ in range(reps):
+            t0 = _t.perf_counter()
+            r = fn()
+            t = min(t, _t.perf_counter() - t0)
+        return r, t
+
+    # whole set: persistent batched vs the static one-job launch
     ctx.run_batch([(wl.seqs, prm)])
-    t0 = _t.perf_counter()
-    res = ctx.run_batch([(wl.seqs, prm)])[0]
-    tb = _t.perf_counter() - t0
+    ctx.run(wl.seqs, prm)
+    rb, tb = best(lambda: ctx.run_batch([(wl.seqs, prm)])[0])
+    rs, ts = best(lambda: ctx.run(wl.seqs, prm))
+    assert rb.motifs == rs.motifs, "batched and static results differ"
+    cells = rb.ref_cells
+    out["whole"] = {"batched_dp_gcups": round(cells / rb.dp_ms / 1e6, 1), "static_dp_gcups": round(cells / rs.dp_ms / 1e6, 1),
+                    "batched_dp_ms": round(rb.dp_ms, 3), "static_dp_ms": round(rs.dp_ms, 3),
+                    "batched_wall_gcups": round(cells / tb / 1e9, 1), "static_wall_gcups": round(cells / ts / 1e9, 1),
+                    "dp_ratio": round(rs.dp_ms / rb.dp_ms, 3), "wall_ratio": round(ts / tb, 3)}
+
+    # many uneven jobs: one batch call vs one motex_gpu_run per job
+    rng = _r.Random(seed)
+    jobs, at = [], 0
+    while at < len(wl.seqs):
+        n = rng.randint(5, 40)
+        jobs.append((wl.seqs[at:at + n], prm))
+        at += n
+    ctx.run_batch(jobs)
+    for s, p in jobs[:3]:
+        ctx.run(s, p)
+    rjb, tjb = best(lambda: ctx.run_batch(jobs))
+    rjs, tjs = best(lambda: [ctx.run(s, p) for s, p in jobs])
+    assert [r.motifs for r in rjb] == [r.motifs for r in rjs], "batched and sequential job results differ"
+    jcells = sum(r.ref_cells for r in rjb)
+    out["jobs"] = {"jobs": len(jobs), "sequences_per_job": "5-40", "batched_gcups": round(jcells / tjb / 1e9, 1),
+                   "sequential_gcups": round(jcells / tjs / 1e9, 1), "batched_ms": round(tjb * 1e3, 2),
+                   "sequential_ms": round(tjs * 1e3, 2), "ratio": round(tjs / tjb, 2)}
+
+    # per-pair drop-in
     seqs = wl.seqs[:sample]
-    cells = 0
+    pcells = 0
     ctx.extract_pair(seqs[0], seqs[1], prm)
     t0 = _t.perf_counter()
     for x in seqs:
         for t in seqs:
             if len(x) >= wl.k and len(t) >= wl.k:
                 ctx.extract_pair(x, t, prm)
-                cells += len(x) * len(t)
+                pcells += len(x) * len(t)
     tp = _t.perf_counter() - t0
-    b, p = res.ref_cells / tb / 1e9, cells / tp / 1e9
-    return {"workload": "prot_uneven_d1", "batched_gcups": round(b, 1), "batched_ms": round(tb * 1e3, 2),
-            "plain_gcups": round(p, 3), "plain_pairs": len(seqs) ** 2, "ratio": round(b / p, 1),
-            "note": "batched: whole set, one persistent DP launch; plain: motex_gpu_extract_pair per ordered pair "
-                    f"of the first {sample} sequences (host wall time, both)"}
+    out["per_pair"] = {"pairs": len(seqs) ** 2, "gcups": round(pcells / tp / 1e9, 3),
+                       "ratio_batched_whole_wall": round(cells / tb / (pcells / tp), 1)}
+    out["note"] = ("whole: one job, batched persistent launch vs static one-job launch (dp = device DP time, "
+                   "wall = host time of the whole call); jobs: one batch call vs motex_gpu_run per job (host "
+                   "wall); per_pair: motex_gpu_extract_pair per ordered pair of the first "
+                   f"{sample} sequences (host wall)")
+    return out
 
 
 def serving(native, nreq=2000, rate_hz=100.0, seed=5, max_batch=32, workers=2):
@@ -345,6 +405,14 @@ def serving(native, nreq=2000, rate_hz=100.0, seed=5, max_batch=32, workers=2):
     out["plain"] = {"p50_ms": round(pct(lat2, 50), 2), "p99_ms": round(pct(lat2, 99), 2),
                     "req_per_s": round(nreq / wall2, 1), "gcups": round(sum(cells) / wall2 / 1e9, 1)}
     return out
+
+
+def workload_config(args, wl, world, l2):
+    """The `config` object of both arms: the workload, its sizes and switches."""
+    return {"workload": args.workload, "scale": args.scale, "alphabet": wl.alphabet, "num_seqs": len(wl.seqs),
+            "total_len": sum(len(s) for s in wl.seqs), "d": wl.d, "k": wl.k, "e": wl.e, "q": wl.q,
+            "boxes": [list(b) for b in wl.boxes], "ref_cells": ref_cells(wl, wl.seqs),
+            "parallelism": f"replicas{world}", "l2": l2}
 
 
 def run_gpu(args, rank, world, local_rank):
@@ -452,11 +520,9 @@ def run_gpu(args, rank, world, local_rank):
         "value": round(value, 2), "unit": "GCUPS", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": round(step_s * 1e3 / args.steps, 3), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "u32 bit-vector (integer)", "data": "synthetic (seeded generator)",
-        "config": {"workload": args.workload, "scale": args.scale, "alphabet": wl.alphabet, "num_seqs": len(wl.seqs),
-                   "total_len": total_pos, "d": wl.d, "k": wl.k, "e": wl.e, "q": wl.q,
-                   "ref_cells": cells, "unique_words": first.unique_words, "motifs": len(first.motifs),
-                   "parallelism": f"replicas{world}", "l2": "flushed (256 MiB write) before every step",
-                   "host_wall_ms_per_step": round(1e3 * statistics.mean(wall), 3)},
+        "config": workload_config(args, wl, world, "flushed (256 MiB write) before every step"),
+        "run": {"unique_words": first.unique_words, "motifs": len(first.motifs),
+                "host_wall_ms_per_step": round(1e3 * statistics.mean(wall), 3)},
         "e2e": {"value": round(e2e, 2), "unit": "GCUPS", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "ms_per_step": round(e2e_s * 1e3 / args.steps, 3)},
         "gpu_launches": launches,
@@ -489,10 +555,8 @@ def run_reference(args, world):
         "value": round(val, 3), "unit": "GCUPS", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": round(secs_t * 1e3 / args.steps, 3), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "integer", "data": "synthetic (seeded generator)",
-        "config": {"workload": args.workload, "scale": args.scale, "alphabet": wl.alphabet, "num_seqs": len(wl.seqs),
-                   "total_len": sum(len(s) for s in wl.seqs), "d": wl.d, "k": wl.k, "e": wl.e, "q": wl.q,
-                   "ref_cells": ref_cells(wl, wl.seqs), "parallelism": f"replicas{world}",
-                   "host_threads": threads},
+        "config": workload_config(args, wl, world, "not applicable (CPU run, host caches)"),
+        "run": {"host_threads": threads},
         "cpu_baseline": {"value": round(val, 3), "unit": "GCUPS", "cores": threads, "kind": kind, "sample": desc},
         "e2e": {"value": round(val, 3), "unit": "GCUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }

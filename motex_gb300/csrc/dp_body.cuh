@@ -527,7 +527,7 @@ __device__ __forceinline__ void dp_swar_body ( const DPArgs & a, const SwarConst
 #pragma unroll
             for ( int b = 0; b < B; ++b ) c |= ( ( __ldg ( planes + ( size_t ) b * stride + k + 1 ) >> lane ) & 1u ) << b;
             rl[lane] = ( TAB ? c : ( c & 7u ) ) * ( W * kDPThreads );
-            rh[lane] = ( c >> 3 ) * ( W * kDPThreads );
+            if constexpr ( ! TAB ) rh[lane] = ( c >> 3 ) * ( W * kDPThreads );     // the high-bit table
         }
         __syncwarp ();
         const uint32_t vm = __ldg ( a.text.vmask + k ), em = __ldg ( a.text.emask + k );

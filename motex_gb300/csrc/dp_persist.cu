@@ -6,31 +6,65 @@
 namespace mtx
 {
 
+/*
+ * Each CTA copies the DPArgs of the job of its current item into shared
+ * memory; the bodies then read the job's pointers and sizes from there once
+ * per text block instead of holding them in registers for the whole item.
+ * The lane constants of the packed bodies (SwarConst) are the same for every
+ * job of a launch (the class key includes l and e) and come in as a kernel
+ * parameter, i.e. from the constant bank like in the one-job kernels.  With
+ * both, the persistent kernels need about the registers of the one-job
+ * kernels.
+ */
+__device__ __forceinline__ void load_job ( const JobDesc * jobs, uint32_t job, DPArgs & s_job )
+{
+    constexpr int kWords = sizeof ( DPArgs ) / sizeof ( uint32_t );
+    static_assert ( sizeof ( DPArgs ) % sizeof ( uint32_t ) == 0, "DPArgs is copied word by word" );
+    const uint32_t * src = reinterpret_cast<const uint32_t *> ( &jobs[job].a );
+    uint32_t * dst = reinterpret_cast<uint32_t *> ( &s_job );
+    for ( int i = threadIdx.x; i < kWords; i += blockDim.x ) dst[i] = src[i];
+    __syncthreads ();
+}
+
 template <int B, int W, bool ED, bool SCALED, int UR>
 __global__ void __launch_bounds__ ( kDPThreads ) k_dp_fast_persist ( const JobDesc * jobs, const WorkItem * items,
                                                                      uint32_t nitems, uint32_t * counter )
 {
+    __shared__ DPArgs s_job;
     WorkItem w;
     while ( next_item ( items, nitems, counter, w ) )
-        dp_fast_body<B, W, ED, SCALED, UR> ( jobs[w.job].a, w.tile, w.chunk );
+    {
+        load_job ( jobs, w.job, s_job );
+        dp_fast_body<B, W, ED, SCALED, UR> ( s_job, w.tile, w.chunk );
+    }
 }
 
 template <int B, int NL, int W, int UR>
 __global__ void __launch_bounds__ ( kDPThreads ) k_dp_hswar_persist ( const JobDesc * jobs, const WorkItem * items,
-                                                                      uint32_t nitems, uint32_t * counter )
+                                                                      uint32_t nitems, uint32_t * counter,
+                                                                      const SwarConst C )
 {
+    __shared__ DPArgs s_job;
     WorkItem w;
     while ( next_item ( items, nitems, counter, w ) )
-        dp_hswar_body<B, NL, W, UR> ( jobs[w.job].a, jobs[w.job].C, w.tile, w.chunk );
+    {
+        load_job ( jobs, w.job, s_job );
+        dp_hswar_body<B, NL, W, UR> ( s_job, C, w.tile, w.chunk );
+    }
 }
 
 template <int B, int NL, int W, int UR>
 __global__ void __launch_bounds__ ( kDPThreads ) k_dp_swar_persist ( const JobDesc * jobs, const WorkItem * items,
-                                                                     uint32_t nitems, uint32_t * counter )
+                                                                     uint32_t nitems, uint32_t * counter,
+                                                                     const SwarConst C )
 {
+    __shared__ DPArgs s_job;
     WorkItem w;
     while ( next_item ( items, nitems, counter, w ) )
-        dp_swar_body<B, NL, W, UR> ( jobs[w.job].a, jobs[w.job].C, w.tile, w.chunk );
+    {
+        load_job ( jobs, w.job, s_job );
+        dp_swar_body<B, NL, W, UR> ( s_job, C, w.tile, w.chunk );
+    }
 }
 
 namespace
@@ -47,7 +81,7 @@ int ctas_per_sm ( K kernel, size_t smem )
 
 template <int B>
 bool launch_b ( const JobDesc * jobs, const WorkItem * items, uint32_t nitems, uint32_t * counter, bool ed, bool scaled,
-                int NL, unsigned grid, cudaStream_t st, int * occ )
+                int NL, const SwarConst & C, unsigned grid, cudaStream_t st, int * occ )
 {
     constexpr int W = 8;
     if ( NL <= 1 )
@@ -83,7 +117,7 @@ bool launch_b ( const JobDesc * jobs, const WorkItem * items, uint32_t nitems, u
         if ( occ ) { *occ = ctas_per_sm ( k_dp_hswar_persist<B, NLV, 8, 4>, smem ); return true; }           \
         cudaFuncSetAttribute ( k_dp_hswar_persist<B, NLV, 8, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize,  \
                                ( int ) smem );                                                              \
-        k_dp_hswar_persist<B, NLV, 8, 4><<<grid, kDPThreads, smem, st>>> ( jobs, items, nitems, counter );    \
+        k_dp_hswar_persist<B, NLV, 8, 4><<<grid, kDPThreads, smem, st>>> ( jobs, items, nitems, counter, C ); \
         return true;                                                                                        \
     }
             switch ( NL )
@@ -106,7 +140,7 @@ bool launch_b ( const JobDesc * jobs, const WorkItem * items, uint32_t nitems, u
         if ( occ ) { *occ = ctas_per_sm ( k_dp_swar_persist<B, NLV, WS, 8>, smem ); return true; }           \
         cudaFuncSetAttribute ( k_dp_swar_persist<B, NLV, WS, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize,  \
                                ( int ) smem );                                                              \
-        k_dp_swar_persist<B, NLV, WS, 8><<<grid, kDPThreads, smem, st>>> ( jobs, items, nitems, counter );    \
+        k_dp_swar_persist<B, NLV, WS, 8><<<grid, kDPThreads, smem, st>>> ( jobs, items, nitems, counter, C ); \
         return true;                                                                                        \
     }
     switch ( NL )
@@ -120,15 +154,15 @@ bool launch_b ( const JobDesc * jobs, const WorkItem * items, uint32_t nitems, u
 }
 
 bool dispatch ( const JobDesc * jobs, const WorkItem * items, uint32_t nitems, uint32_t * counter, int B, bool ed,
-                bool scaled, int NL, unsigned grid, cudaStream_t st, int * occ )
+                bool scaled, int NL, const SwarConst & C, unsigned grid, cudaStream_t st, int * occ )
 {
     switch ( B )
     {
         case 1:
-        case 2: return launch_b<2> ( jobs, items, nitems, counter, ed, scaled, NL, grid, st, occ );
-        case 3: return launch_b<3> ( jobs, items, nitems, counter, ed, scaled, NL, grid, st, occ );
-        case 4: return launch_b<4> ( jobs, items, nitems, counter, ed, scaled, NL, grid, st, occ );
-        case 5: return launch_b<5> ( jobs, items, nitems, counter, ed, scaled, NL, grid, st, occ );
+        case 2: return launch_b<2> ( jobs, items, nitems, counter, ed, scaled, NL, C, grid, st, occ );
+        case 3: return launch_b<3> ( jobs, items, nitems, counter, ed, scaled, NL, C, grid, st, occ );
+        case 4: return launch_b<4> ( jobs, items, nitems, counter, ed, scaled, NL, C, grid, st, occ );
+        case 5: return launch_b<5> ( jobs, items, nitems, counter, ed, scaled, NL, C, grid, st, occ );
         default: return false;
     }
 }
@@ -138,14 +172,14 @@ bool dispatch ( const JobDesc * jobs, const WorkItem * items, uint32_t nitems, u
 int persistent_ctas_per_sm ( int B, bool ed, bool scaled, int NL, int, int )
 {
     int occ = 1;
-    if ( ! dispatch ( nullptr, nullptr, 0, nullptr, B, ed, scaled, NL, 0, nullptr, &occ ) ) return 1;
+    if ( ! dispatch ( nullptr, nullptr, 0, nullptr, B, ed, scaled, NL, SwarConst {}, 0, nullptr, &occ ) ) return 1;
     return occ;
 }
 
 bool launch_dp_persistent ( const JobDesc * jobs, const WorkItem * items, uint32_t nitems, uint32_t * counter, int B,
-                            bool ed, bool scaled, int NL, int, int, unsigned grid, cudaStream_t st )
+                            bool ed, bool scaled, int NL, const SwarConst & C, unsigned grid, cudaStream_t st )
 {
-    return dispatch ( jobs, items, nitems, counter, B, ed, scaled, NL, grid, st, nullptr );
+    return dispatch ( jobs, items, nitems, counter, B, ed, scaled, NL, C, grid, st, nullptr );
 }
 
 } // namespace mtx

@@ -377,7 +377,10 @@ __global__ void k_gather_key ( const uint32_t * __restrict__ idx, uint32_t n, co
     key_out[i] = ( uint32_t ) acc;
 }
 
-// Per-tile digit histogram, digit-major: hist[d * ntiles + tile].
+// Per-tile digit histogram, digit-major: hist[d * ntiles + tile].  Keys are
+// read as 16-byte vectors where the tile allows; equal digits within a warp
+// are counted by one shared atomic of their leader (repetitive inputs put
+// most keys of a warp on a few digits).
 __global__ void __launch_bounds__ ( kSortThreads ) k_radix_hist ( const uint32_t * __restrict__ keys, uint32_t n,
                                                                    int shift, uint32_t * hist, uint32_t ntiles )
 {
@@ -385,20 +388,48 @@ __global__ void __launch_bounds__ ( kSortThreads ) k_radix_hist ( const uint32_t
     for ( int d = threadIdx.x; d < 256; d += kSortThreads ) cnt[d] = 0;
     __syncthreads ();
     const uint32_t base = blockIdx.x * kSortTile;
-#pragma unroll 4
-    for ( int r = 0; r < kSortItems; ++r )
+    const uint32_t lt = lanemask_lt ();
+    auto add = [&] ( bool valid, uint32_t k ) {
+        const uint32_t d = valid ? ( ( k >> shift ) & 255u ) : 256u;
+        const uint32_t peers = __match_any_sync ( 0xffffffffu, d );
+        if ( valid && ( peers & lt ) == 0 ) atomicAdd ( &cnt[d], __popc ( peers ) );
+    };
+    if ( base + kSortTile <= n )
     {
-        uint32_t i = base + r * kSortThreads + threadIdx.x;
-        if ( i < n ) atomicAdd ( &cnt[( keys[i] >> shift ) & 255u], 1u );
+        const uint4 * k4 = reinterpret_cast<const uint4 *> ( keys + base );
+#pragma unroll
+        for ( int r = 0; r < kSortItems / 4; ++r )
+        {
+            const uint4 q = __ldg ( k4 + r * kSortThreads + threadIdx.x );
+            add ( true, q.x );
+            add ( true, q.y );
+            add ( true, q.z );
+            add ( true, q.w );
+        }
+    }
+    else
+    {
+        for ( int r = 0; r < kSortItems; ++r )
+        {
+            const uint32_t i = base + r * kSortThreads + threadIdx.x;
+            add ( i < n, i < n ? keys[i] : 0u );
+        }
     }
     __syncthreads ();
     for ( int d = threadIdx.x; d < 256; d += kSortThreads ) hist[( size_t ) d * ntiles + blockIdx.x] = cnt[d];
 }
 
 /*
- * Stable scatter of one 8-bit digit.  Items are visited in input order
- * (round r, then thread index); ranks among equal digits come from warp
- * match masks plus per-warp counts, so equal keys keep their order.
+ * Stable scatter of one 8-bit digit.  The CTA first sorts its tile by the
+ * digit in shared memory: items are ranked in input order (round r, then
+ * thread index; ranks among equal digits from warp match masks plus per-warp
+ * counts) and stored at their digit's tile-local offset.  Then consecutive
+ * threads write consecutive items of the locally sorted tile, so every
+ * digit's run of the tile leaves as contiguous stores instead of scattered
+ * 4-byte writes.  The tile's digit counts and global bases come from the
+ * digit-major scanned histogram: offsets[d * ntiles + t] is the first output
+ * slot of digit d from tile t, and the next entry of the flattened array
+ * (or n after the last) ends it.
  */
 __global__ void __launch_bounds__ ( kSortThreads ) k_radix_scatter ( const uint32_t * __restrict__ keys_in,
                                                                       const uint32_t * __restrict__ vals_in,
@@ -409,26 +440,50 @@ __global__ void __launch_bounds__ ( kSortThreads ) k_radix_scatter ( const uint3
                                                                       uint32_t ntiles )
 {
     constexpr int NW = kSortThreads / 32;
-    __shared__ uint32_t s_base[256];
+    __shared__ uint32_t s_base[256];                 // global first slot of digit d from this tile
+    __shared__ uint32_t s_start[256];                // tile-local first slot of digit d
     __shared__ uint32_t s_run[256];
     __shared__ uint32_t s_wcnt[NW][256];
+    __shared__ uint32_t s_wtot[NW];
+    __shared__ uint32_t s_key[kSortTile];
+    __shared__ uint32_t s_val[kSortTile];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    for ( int d = threadIdx.x; d < 256; d += kSortThreads )
+    const uint32_t tile = blockIdx.x;
+    const uint32_t base = tile * kSortTile;
+    const uint32_t tn = min ( ( uint32_t ) kSortTile, n - base );
+    const uint32_t nhist = 256u * ntiles;
+    // tile-local digit counts from the scanned histogram, then their exclusive
+    // scan over the 256 digits (one digit per thread, warp scans + warp totals)
     {
-        s_base[d] = offsets[( size_t ) d * ntiles + blockIdx.x];
+        const uint32_t d = threadIdx.x;                          // kSortThreads == 256
+        const size_t f = ( size_t ) d * ntiles + tile;
+        const uint32_t b = offsets[f];
+        const uint32_t c = ( f + 1 < nhist ? offsets[f + 1] : n ) - b;
+        s_base[d] = b;
         s_run[d] = 0;
 #pragma unroll
         for ( int w = 0; w < NW; ++w ) s_wcnt[w][d] = 0;
+        uint32_t x = c;
+#pragma unroll
+        for ( int o = 1; o < 32; o <<= 1 )
+        {
+            const uint32_t y = __shfl_up_sync ( 0xffffffffu, x, o );
+            if ( lane >= o ) x += y;
+        }
+        if ( lane == 31 ) s_wtot[warp] = x;                      // warp total
+        __syncthreads ();
+        uint32_t add = 0;
+        for ( int w = 0; w < warp; ++w ) add += s_wtot[w];
+        s_start[d] = add + x - c;                                // exclusive over all digits
     }
     __syncthreads ();
-    const uint32_t base = blockIdx.x * kSortTile;
     const uint32_t lt = lanemask_lt ();
     for ( int r = 0; r < kSortItems; ++r )
     {
-        const uint32_t i = base + r * kSortThreads + threadIdx.x;
-        const bool valid = i < n;
-        const uint32_t k = valid ? keys_in[i] : 0u;
-        const uint32_t v = valid ? vals_in[i] : 0u;
+        const uint32_t li = r * kSortThreads + threadIdx.x;
+        const bool valid = li < tn;
+        const uint32_t k = valid ? keys_in[base + li] : 0u;
+        const uint32_t v = valid ? vals_in[base + li] : 0u;
         const uint32_t d = valid ? ( ( k >> shift ) & 255u ) : ( 256u + lane );
         const uint32_t peers = __match_any_sync ( 0xffffffffu, d );
         const uint32_t rank = __popc ( peers & lt );
@@ -438,9 +493,9 @@ __global__ void __launch_bounds__ ( kSortThreads ) k_radix_scatter ( const uint3
         {
             uint32_t off = s_run[d];
             for ( int w = 0; w < warp; ++w ) off += s_wcnt[w][d];
-            const uint32_t dst = s_base[d] + off + rank;
-            keys_out[dst] = k;
-            vals_out[dst] = v;
+            const uint32_t pos = s_start[d] + off + rank;
+            s_key[pos] = k;
+            s_val[pos] = v;
         }
         __syncthreads ();
         for ( int dd = threadIdx.x; dd < 256; dd += kSortThreads )
@@ -455,6 +510,15 @@ __global__ void __launch_bounds__ ( kSortThreads ) k_radix_scatter ( const uint3
             s_run[dd] += t;
         }
         __syncthreads ();
+    }
+    // the locally sorted tile: item i of digit d goes to s_base[d] + (i - s_start[d])
+    for ( uint32_t i = threadIdx.x; i < tn; i += kSortThreads )
+    {
+        const uint32_t k = s_key[i];
+        const uint32_t d = ( k >> shift ) & 255u;
+        const uint32_t dst = s_base[d] + ( i - s_start[d] );
+        keys_out[dst] = k;
+        vals_out[dst] = s_val[i];
     }
 }
 

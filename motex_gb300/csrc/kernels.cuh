@@ -227,10 +227,11 @@ struct WorkItem
     uint32_t job, tile, chunk;
 };
 
-// Persistent batched DP: kind 0 = 1-lane kernels (Hamming or edit distance),
-// kind 1 = SWAR edit distance with NL lanes.  grid = resident CTA slots.
+// Persistent batched DP over the items of one kernel class: 1-lane kernels
+// (NL = 1, Hamming or edit distance) or packed ones (NL lanes; every job of
+// the launch has the lane constants C).  grid = resident CTA slots.
 bool launch_dp_persistent ( const JobDesc * jobs, const WorkItem * items, uint32_t nitems, uint32_t * counter,
-                            int B, bool ed, bool scaled, int NL, int W, int UR, unsigned grid, cudaStream_t st );
+                            int B, bool ed, bool scaled, int NL, const SwarConst & C, unsigned grid, cudaStream_t st );
 int persistent_ctas_per_sm ( int B, bool ed, bool scaled, int NL, int W, int UR );
 
 // Edit distance, NL = swar_lanes(l) >= 2 factors per 32-bit register (l <= 15);

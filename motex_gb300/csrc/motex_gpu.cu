@@ -1418,14 +1418,17 @@ int fetch_records ( Job * j, motex_result * out )
  */
 int batch_dp ( motex_ctx * c, std::vector<Job *> & jobs, float * dp_ms )
 {
+    // packed classes also key on l and e: their lane constants are a kernel
+    // parameter shared by every job of the launch
     struct Class
     {
         int B;
         bool ed, scaled;
         int NL;
+        uint32_t l, e;
         bool operator< ( const Class & o ) const
         {
-            return std::tie ( B, ed, scaled, NL ) < std::tie ( o.B, o.ed, o.scaled, o.NL );
+            return std::tie ( B, ed, scaled, NL, l, e ) < std::tie ( o.B, o.ed, o.scaled, o.NL, o.l, o.e );
         }
     };
     std::map<Class, std::vector<Job *>> classes;
@@ -1439,7 +1442,9 @@ int batch_dp ( motex_ctx * c, std::vector<Job *> & jobs, float * dp_ms )
             continue;
         }
         const bool ed = j->prm.d == 1;
-        Class k { j->B < 2 ? 2 : j->B, ed, ed && j->prm.l <= 28 && j->tune.NL == 1, j->tune.NL };
+        const bool packed = j->tune.NL > 1;
+        Class k { j->B < 2 ? 2 : j->B, ed, ed && j->prm.l <= 28 && j->tune.NL == 1, j->tune.NL,
+                  packed ? j->prm.l : 0u, packed && ed ? j->prm.e : 0u };
         // register words per thread of the persistent kernels
         j->tune.W = ( j->tune.NL > 1 && ed ) ? swar_default_w ( k.B ) : 8;
         const uint32_t groups = ( j->U + j->tune.NL - 1 ) / j->tune.NL;
@@ -1499,7 +1504,7 @@ int batch_dp ( motex_ctx * c, std::vector<Job *> & jobs, float * dp_ms )
             const int per_sm = persistent_ctas_per_sm ( k.B, k.ed, k.scaled, k.NL, 8, 8 );
             const unsigned grid = ( unsigned ) std::min<size_t> ( cn, ( size_t ) per_sm * c->num_sms );
             if ( ! launch_dp_persistent ( dj + jfirst, di + ifirst, ( uint32_t ) cn, dcount + ci, k.B, k.ed, k.scaled,
-                                          k.NL, 8, 8, grid, c->st ) )
+                                          k.NL, hj[jfirst].C, grid, c->st ) )
                 return fail ( MOTEX_EUNSUPPORTED, "no persistent DP kernel for this class" );
             c->launches++;
             cudaError_t e = cudaGetLastError ();

@@ -45,5 +45,9 @@ def test_reference_arm_line(monkeypatch):
     for key in ("workload", "scale", "alphabet", "num_seqs", "total_len", "d", "k", "e", "q", "ref_cells", "parallelism"):
         assert key in cfg, key
     assert cfg["ref_cells"] == 32000 * 32000                 # 64 x 500 nt, every sequence searched
+    # the GPU arm builds its config with the same function: identical keys
+    gpu_cfg = bench.workload_config(args, bench.WORKLOADS["dna_hd_small"](1.0), 2, "flushed")
+    assert set(cfg) == set(gpu_cfg)
+    assert {k: v for k, v in cfg.items() if k != "l2"} == {k: v for k, v in gpu_cfg.items() if k != "l2"}
     assert line["e2e"]["value"] == line["value"] == line["cpu_baseline"]["value"]
     assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["e2e"]["d2h_bytes_per_step"] == 0

@@ -3,6 +3,8 @@
 // device counter (see next_item in dp_body.cuh).
 #include "dp_body.cuh"
 
+#include <type_traits>
+
 namespace mtx
 {
 
@@ -81,27 +83,26 @@ int ctas_per_sm ( K kernel, size_t smem )
 
 template <int B>
 bool launch_b ( const JobDesc * jobs, const WorkItem * items, uint32_t nitems, uint32_t * counter, bool ed, bool scaled,
-                int NL, const SwarConst & C, unsigned grid, cudaStream_t st, int * occ )
+                int NL, int W, int UR, const SwarConst & C, unsigned grid, cudaStream_t st, int * occ )
 {
-    constexpr int W = 8;
     if ( NL <= 1 )
     {
         if ( ! ed )
         {
-            if ( occ ) { *occ = ctas_per_sm ( k_dp_fast_persist<B, W, false, false, 4>, 0 ); return true; }
-            k_dp_fast_persist<B, W, false, false, 4><<<grid, kDPThreads, 0, st>>> ( jobs, items, nitems, counter );
+            if ( occ ) { *occ = ctas_per_sm ( k_dp_fast_persist<B, 8, false, false, 4>, 0 ); return true; }
+            k_dp_fast_persist<B, 8, false, false, 4><<<grid, kDPThreads, 0, st>>> ( jobs, items, nitems, counter );
         }
         else if ( scaled )
         {
-            const size_t smem = fast_smem_bytes ( B, W, true );
-            if ( occ ) { *occ = ctas_per_sm ( k_dp_fast_persist<B, W, true, true, 8>, smem ); return true; }
-            k_dp_fast_persist<B, W, true, true, 8><<<grid, kDPThreads, smem, st>>> ( jobs, items, nitems, counter );
+            const size_t smem = fast_smem_bytes ( B, 8, true );
+            if ( occ ) { *occ = ctas_per_sm ( k_dp_fast_persist<B, 8, true, true, 8>, smem ); return true; }
+            k_dp_fast_persist<B, 8, true, true, 8><<<grid, kDPThreads, smem, st>>> ( jobs, items, nitems, counter );
         }
         else
         {
-            const size_t smem = fast_smem_bytes ( B, W, true );
-            if ( occ ) { *occ = ctas_per_sm ( k_dp_fast_persist<B, W, true, false, 8>, smem ); return true; }
-            k_dp_fast_persist<B, W, true, false, 8><<<grid, kDPThreads, smem, st>>> ( jobs, items, nitems, counter );
+            const size_t smem = fast_smem_bytes ( B, 8, true );
+            if ( occ ) { *occ = ctas_per_sm ( k_dp_fast_persist<B, 8, true, false, 8>, smem ); return true; }
+            k_dp_fast_persist<B, 8, true, false, 8><<<grid, kDPThreads, smem, st>>> ( jobs, items, nitems, counter );
         }
         return true;
     }
@@ -132,54 +133,70 @@ bool launch_b ( const JobDesc * jobs, const WorkItem * items, uint32_t nitems, u
         }
         return false;
     }
-#define MTX_SWAR_P( NLV )                                                                                   \
-    case NLV:                                                                                               \
-    {                                                                                                       \
-        constexpr int WS = swar_default_w ( B );                                                            \
-        const size_t smem = swar_smem_bytes ( B, NLV, WS );                                                 \
-        if ( occ ) { *occ = ctas_per_sm ( k_dp_swar_persist<B, NLV, WS, 8>, smem ); return true; }           \
-        cudaFuncSetAttribute ( k_dp_swar_persist<B, NLV, WS, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize,  \
-                               ( int ) smem );                                                              \
-        k_dp_swar_persist<B, NLV, WS, 8><<<grid, kDPThreads, smem, st>>> ( jobs, items, nitems, counter, C ); \
-        return true;                                                                                        \
-    }
+    // packed edit distance: every (W, UR) the autotuner may pick for the one-job kernel
+    auto swar = [&] ( auto nl, auto w, auto ur ) -> bool {
+        constexpr int NLV = decltype ( nl )::value, WV = decltype ( w )::value, URV = decltype ( ur )::value;
+        const size_t smem = swar_smem_bytes ( B, NLV, WV );
+        if ( occ ) { *occ = ctas_per_sm ( k_dp_swar_persist<B, NLV, WV, URV>, smem ); return true; }
+        cudaFuncSetAttribute ( k_dp_swar_persist<B, NLV, WV, URV>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               ( int ) smem );
+        k_dp_swar_persist<B, NLV, WV, URV><<<grid, kDPThreads, smem, st>>> ( jobs, items, nitems, counter, C );
+        return true;
+    };
+    auto swar_nl = [&] ( auto nl ) -> bool {
+        using I4 = std::integral_constant<int, 4>;
+        using I8 = std::integral_constant<int, 8>;
+        if ( W == 4 && UR == 4 ) return swar ( nl, I4 {}, I4 {} );
+        if ( W == 4 && UR == 8 ) return swar ( nl, I4 {}, I8 {} );
+        if ( W == 8 && UR == 4 ) return swar ( nl, I8 {}, I4 {} );
+        if ( W == 8 && UR == 8 ) return swar ( nl, I8 {}, I8 {} );
+        return false;
+    };
     switch ( NL )
     {
-        MTX_SWAR_P ( 2 )
-        MTX_SWAR_P ( 3 )
-        MTX_SWAR_P ( 4 )
+        case 2: return swar_nl ( std::integral_constant<int, 2> {} );
+        case 3: return swar_nl ( std::integral_constant<int, 3> {} );
+        case 4: return swar_nl ( std::integral_constant<int, 4> {} );
         default: return false;
     }
-#undef MTX_SWAR_P
 }
 
 bool dispatch ( const JobDesc * jobs, const WorkItem * items, uint32_t nitems, uint32_t * counter, int B, bool ed,
-                bool scaled, int NL, const SwarConst & C, unsigned grid, cudaStream_t st, int * occ )
+                bool scaled, int NL, int W, int UR, const SwarConst & C, unsigned grid, cudaStream_t st, int * occ )
 {
     switch ( B )
     {
         case 1:
-        case 2: return launch_b<2> ( jobs, items, nitems, counter, ed, scaled, NL, C, grid, st, occ );
-        case 3: return launch_b<3> ( jobs, items, nitems, counter, ed, scaled, NL, C, grid, st, occ );
-        case 4: return launch_b<4> ( jobs, items, nitems, counter, ed, scaled, NL, C, grid, st, occ );
-        case 5: return launch_b<5> ( jobs, items, nitems, counter, ed, scaled, NL, C, grid, st, occ );
+        case 2: return launch_b<2> ( jobs, items, nitems, counter, ed, scaled, NL, W, UR, C, grid, st, occ );
+        case 3: return launch_b<3> ( jobs, items, nitems, counter, ed, scaled, NL, W, UR, C, grid, st, occ );
+        case 4: return launch_b<4> ( jobs, items, nitems, counter, ed, scaled, NL, W, UR, C, grid, st, occ );
+        case 5: return launch_b<5> ( jobs, items, nitems, counter, ed, scaled, NL, W, UR, C, grid, st, occ );
         default: return false;
     }
 }
 
 } // namespace
 
-int persistent_ctas_per_sm ( int B, bool ed, bool scaled, int NL, int, int )
+int persistent_ctas_per_sm ( int B, bool ed, bool scaled, int NL, int W, int UR )
 {
     int occ = 1;
-    if ( ! dispatch ( nullptr, nullptr, 0, nullptr, B, ed, scaled, NL, SwarConst {}, 0, nullptr, &occ ) ) return 1;
+    if ( ! dispatch ( nullptr, nullptr, 0, nullptr, B, ed, scaled, NL, W, UR, SwarConst {}, 0, nullptr, &occ ) )
+        return 1;
     return occ;
 }
 
-bool launch_dp_persistent ( const JobDesc * jobs, const WorkItem * items, uint32_t nitems, uint32_t * counter, int B,
-                            bool ed, bool scaled, int NL, const SwarConst & C, unsigned grid, cudaStream_t st )
+bool persistent_shape ( int B, bool ed, int NL, int W, int UR )
 {
-    return dispatch ( jobs, items, nitems, counter, B, ed, scaled, NL, C, grid, st, nullptr );
+    if ( NL <= 1 ) return W == 8 && UR == ( ed ? 8 : 4 );
+    if ( ! ed ) return B >= 3 && W == 8 && UR == 4;
+    return ( W == 4 || W == 8 ) && ( UR == 4 || UR == 8 );
+}
+
+bool launch_dp_persistent ( const JobDesc * jobs, const WorkItem * items, uint32_t nitems, uint32_t * counter, int B,
+                            bool ed, bool scaled, int NL, int W, int UR, const SwarConst & C, unsigned grid,
+                            cudaStream_t st )
+{
+    return dispatch ( jobs, items, nitems, counter, B, ed, scaled, NL, W, UR, C, grid, st, nullptr );
 }
 
 } // namespace mtx

@@ -411,8 +411,8 @@ DPTune choose_tune ( Job * j, uint32_t U, bool ed, bool generic )
  * chunks as fill every SM's CTA slots several times, like the real grid, and
  * long enough that the per-CTA set-up weighs as little as in the real run;
  * time per cell from CUDA events picks the winner; accumulators are cleared
- * afterwards.  Batched jobs are not tuned (the persistent kernels
- * have a fixed shape).  Entries are shared by every context of the
+ * afterwards.  A batched job's entry also picks the shape of the
+ * persistent kernel its class runs (where one implements it).  Entries are shared by every context of the
  * process and, with MOTEX_TUNE_CACHE=<file>, read from and appended to that
  * file.  MOTEX_AUTOTUNE=0 turns tuning off (the defaults of choose_tune
  * apply); explicit MOTEX_DP_* overrides win over both.
@@ -767,7 +767,9 @@ int stage_plan ( Job * j, bool sorted )
     da.neg1 = ~0u;
     if ( ! j->replaying ) j->tune = choose_tune ( j, U, ed, j->generic );
     bool tune_now = false;
-    if ( ! j->replaying && ! j->generic && ! j->batched && ! getenv ( "MOTEX_DP_W" ) && ! getenv ( "MOTEX_DP_UR" ) &&
+    // batched jobs tune too: the key's entry then also picks the persistent
+    // kernel's shape (batch_dp)
+    if ( ! j->replaying && ! j->generic && ! getenv ( "MOTEX_DP_W" ) && ! getenv ( "MOTEX_DP_UR" ) &&
          ! getenv ( "MOTEX_DP_SWAR" ) )
     {
         const char * at = getenv ( "MOTEX_AUTOTUNE" );
@@ -1426,9 +1428,10 @@ int batch_dp ( motex_ctx * c, std::vector<Job *> & jobs, float * dp_ms )
         bool ed, scaled;
         int NL;
         uint32_t l, e;
+        int W, UR;
         bool operator< ( const Class & o ) const
         {
-            return std::tie ( B, ed, scaled, NL, l, e ) < std::tie ( o.B, o.ed, o.scaled, o.NL, o.l, o.e );
+            return std::tie ( B, ed, scaled, NL, l, e, W, UR ) < std::tie ( o.B, o.ed, o.scaled, o.NL, o.l, o.e, o.W, o.UR );
         }
     };
     std::map<Class, std::vector<Job *>> classes;
@@ -1442,11 +1445,24 @@ int batch_dp ( motex_ctx * c, std::vector<Job *> & jobs, float * dp_ms )
             continue;
         }
         const bool ed = j->prm.d == 1;
+        const int Bc = j->B < 2 ? 2 : j->B;
+        // launch shape: the autotuner's entry for the key (from this process
+        // or the tune cache) where a persistent kernel implements it, else
+        // the persistent defaults (packed edit distance: W by bit planes,
+        // unroll 8; otherwise W = 8 with the kernel's unroll)
+        DPTune t;
+        const bool tuned = ! getenv ( "MOTEX_DP_W" ) && ! getenv ( "MOTEX_DP_UR" ) && ! getenv ( "MOTEX_DP_SWAR" ) &&
+                           tune_lookup ( TuneKey { j->B, j->prm.l, j->prm.e, j->prm.d }, &t ) &&
+                           persistent_shape ( Bc, ed, t.NL, t.W, t.UR );
+        if ( tuned ) j->tune = t;
+        else
+        {
+            j->tune.W = ( j->tune.NL > 1 && ed ) ? swar_default_w ( Bc ) : 8;
+            j->tune.UR = ( j->tune.NL > 1 ? ( ed ? 8 : 4 ) : ( ed ? 8 : 4 ) );
+        }
         const bool packed = j->tune.NL > 1;
-        Class k { j->B < 2 ? 2 : j->B, ed, ed && j->prm.l <= 28 && j->tune.NL == 1, j->tune.NL,
-                  packed ? j->prm.l : 0u, packed && ed ? j->prm.e : 0u };
-        // register words per thread of the persistent kernels
-        j->tune.W = ( j->tune.NL > 1 && ed ) ? swar_default_w ( k.B ) : 8;
+        Class k { Bc, ed, ed && j->prm.l <= 28 && j->tune.NL == 1, j->tune.NL,
+                  packed ? j->prm.l : 0u, packed && ed ? j->prm.e : 0u, j->tune.W, j->tune.UR };
         const uint32_t groups = ( j->U + j->tune.NL - 1 ) / j->tune.NL;
         j->ntiles = ( groups + kDPThreads * j->tune.W - 1 ) / ( kDPThreads * j->tune.W );
         classes[k].push_back ( j );
@@ -1501,10 +1517,10 @@ int batch_dp ( motex_ctx * c, std::vector<Job *> & jobs, float * dp_ms )
                                          cudaMemcpyHostToDevice, c->st ) );
             MTX_CUDA ( cudaMemcpyAsync ( di + ifirst, hi + ifirst, cn * sizeof ( WorkItem ), cudaMemcpyHostToDevice, c->st ) );
             const Class & k = kv.first;
-            const int per_sm = persistent_ctas_per_sm ( k.B, k.ed, k.scaled, k.NL, 8, 8 );
+            const int per_sm = persistent_ctas_per_sm ( k.B, k.ed, k.scaled, k.NL, k.W, k.UR );
             const unsigned grid = ( unsigned ) std::min<size_t> ( cn, ( size_t ) per_sm * c->num_sms );
             if ( ! launch_dp_persistent ( dj + jfirst, di + ifirst, ( uint32_t ) cn, dcount + ci, k.B, k.ed, k.scaled,
-                                          k.NL, hj[jfirst].C, grid, c->st ) )
+                                          k.NL, k.W, k.UR, hj[jfirst].C, grid, c->st ) )
                 return fail ( MOTEX_EUNSUPPORTED, "no persistent DP kernel for this class" );
             c->launches++;
             cudaError_t e = cudaGetLastError ();

@@ -216,6 +216,40 @@ bool launch_dp_hswar ( const DPArgs & a, int B, int NL, int W, int UR, dim3 grid
 // distance, k 10: W = 4 runs 352 ms, W = 8 393 ms).
 __host__ __device__ constexpr int swar_default_w ( int B ) { return B >= 4 ? 4 : 8; }
 
+// Small-job pipeline (mini.cu): one CTA per job runs every stage around the
+// DP.  The host fills one MiniJob per job; result[0..2] receive the error
+// flag, the distinct-factor count U and the motif count.
+constexpr int kMiniThreads = 1024;
+constexpr uint32_t kMiniMaxSymbols = 131072;
+struct MiniJob
+{
+    const uint8_t *      raw;
+    const uint32_t *     offs;           // nseq + 1
+    const uint8_t *      qok;            // nseq + 1
+    uint32_t             nseq, total, l, tml, vstart, B, nmin, nmax, n_split;
+    uint32_t             nblk, plane_stride, tbits;
+    int                  top_aligned;    // Hamming factor planes
+    uint8_t *            codes;
+    uint32_t *           planes;
+    uint32_t *           vmask;
+    uint32_t *           emask;
+    unsigned long long * tkey;           // 2^tbits hash slots
+    uint32_t *           tpos;
+    uint32_t *           uniq;           // first end position of every distinct factor
+    uint32_t *           wpl;            // [b * U + w]
+    uint32_t *           u_acc;
+    uint32_t *           v_acc;
+    uint8_t *            flags;          // n_split rows of U
+    uint8_t *            mark;           // total
+    uint32_t *           rec_u;
+    uint32_t *           rec_v;
+    uint32_t *           recs;           // 3 words per motif
+    uint32_t *           result;
+    uint8_t              cmap[256];
+};
+__global__ void k_mini_prep ( const MiniJob * jobs );
+__global__ void k_mini_post ( const MiniJob * jobs );
+
 // One job of a batched launch and one unit of its work.
 struct JobDesc
 {

@@ -156,6 +156,9 @@ struct motex_ctx
     DevBuf bjobs, bitems, bcounter;
     void * bpinned = nullptr;
     size_t bpinned_cap = 0;
+    DevBuf mjobs, mres;                        // small-job pipeline: descriptors, result words
+    void * mpinned = nullptr;
+    size_t mpinned_cap = 0;
     cudaEvent_t evb0 = nullptr, evb1 = nullptr;
 };
 
@@ -1352,7 +1355,32 @@ int load_job ( Job * j, const motex_params * prm, const char * const * seqs, con
     return MOTEX_OK;
 }
 
+// Queue the copy of the job's records into its pinned stage.
+int fetch_issue ( Job * j )
+{
+    if ( j->nrec == 0 ) return MOTEX_OK;
+    const size_t bytes = ( size_t ) j->nrec * 12;
+    MTX_TRY ( ensure_pinned ( j, kPinStage + bytes ) );
+    MTX_CUDA ( cudaMemcpyAsync ( pin<uint32_t> ( j, kPinStage ), dptr<uint32_t> ( j, S_RECS ), bytes,
+                                 cudaMemcpyDeviceToHost, j->ctx->st ) );
+    return MOTEX_OK;
+}
+
+// The result from the copied records (the copy has completed).
+int fetch_build ( Job * j, motex_result * out );
+
 int fetch_records ( Job * j, motex_result * out )
+{
+    if ( j->nrec )
+    {
+        MTX_TRY ( sync ( j->ctx ) );
+        MTX_TRY ( fetch_issue ( j ) );
+        MTX_TRY ( sync ( j->ctx ) );
+    }
+    return fetch_build ( j, out );
+}
+
+int fetch_build ( Job * j, motex_result * out )
 {
     memset ( out, 0, sizeof *out );
     out->num_seqs = j->nseq;
@@ -1363,12 +1391,7 @@ int fetch_records ( Job * j, motex_result * out )
     out->device_ms = j->device_ms;
     out->dp_ms = j->dp_ms;
     if ( j->nrec == 0 ) return MOTEX_OK;
-    const size_t bytes = ( size_t ) j->nrec * 12;
-    MTX_TRY ( sync ( j->ctx ) );
-    MTX_TRY ( ensure_pinned ( j, kPinStage + bytes ) );
-    uint32_t * h = pin<uint32_t> ( j, kPinStage );
-    MTX_CUDA ( cudaMemcpyAsync ( h, dptr<uint32_t> ( j, S_RECS ), bytes, cudaMemcpyDeviceToHost, j->ctx->st ) );
-    MTX_TRY ( sync ( j->ctx ) );
+    const uint32_t * h = pin<uint32_t> ( j, kPinStage );
     out->motifs = static_cast<motex_motif *> ( malloc ( ( size_t ) j->nrec * sizeof ( motex_motif ) ) );
     if ( ! out->motifs ) return fail ( MOTEX_ENOMEM, "host allocation of the result failed" );
     const uint32_t G = j->prm.nb_gaps ? j->G : 1;
@@ -1535,6 +1558,188 @@ int batch_dp ( motex_ctx * c, std::vector<Job *> & jobs, float * dp_ms )
     return MOTEX_OK;
 }
 
+// ------------------------------------------------------- small jobs
+
+/*
+ * Whether a loaded job takes the small-job pipeline (mini.cu): a whole-set
+ * run of plain motifs of at most kMiniMaxSymbols symbols whose factors pack
+ * into 63 bits.  Its alphabet (code map and bit planes B) is taken here from
+ * the staged input, which also spares the presence kernel and its sync.
+ * MOTEX_MINI=0 sends every job down the staged pipeline.
+ */
+bool mini_eligible ( Job * j )
+{
+    const motex_params & P = j->prm;
+    if ( const char * e = getenv ( "MOTEX_MINI" ) )
+        if ( atoi ( e ) == 0 ) return false;
+    if ( j->npat || P.nb_gaps || P.l > 31 || j->total > kMiniMaxSymbols ) return false;
+    const uint8_t * raw = pin<uint8_t> ( j, kPinStage );          // load_job staged the input here
+    uint8_t seen[256] = {};
+    for ( uint64_t i = 0; i < j->total; ++i ) seen[raw[i]] = 1;
+    uint8_t * cmap = pin<uint8_t> ( j, kPinCmap );
+    uint32_t sigma = 0;
+    for ( int i = 0; i < 256; ++i ) cmap[i] = seen[i] ? ( uint8_t ) sigma++ : 0;
+    int B = 2;                                      // one- and two-symbol inputs run on the 2-plane kernels
+    while ( ( 1u << B ) < sigma ) ++B;
+    if ( B > kMaxPlanes || P.l * ( uint32_t ) B > 63 ) return false;
+    j->B = B;
+    return true;
+}
+
+/*
+ * The small-job pipeline for loaded, eligible jobs: k_mini_prep (one CTA per
+ * job) -> sync (distinct-factor counts) -> the DP (the job's static launch
+ * when alone, the batch's persistent launches otherwise) -> k_mini_post ->
+ * sync (motif counts) -> record copies queued -> sync.  The caller reads the
+ * times and builds the results.
+ */
+int run_mini ( motex_ctx * c, std::vector<Job *> & js, float * dp_ms )
+{
+    const uint32_t n = ( uint32_t ) js.size ();
+    cudaStream_t st = c->st;
+    *dp_ms = 0.f;
+    // text chunks: enough (job, tile, chunk) items to fill the GPU, tiles
+    // estimated from the factor counts (the distinct count is not known yet)
+    uint64_t tiles_all = 0;
+    for ( Job * j : js )
+    {
+        const DPTune t = choose_tune ( j, std::max<uint32_t> ( 1, j->nwords ), j->prm.d == 1, false );
+        const uint32_t groups = ( j->nwords + t.NL - 1 ) / t.NL;
+        tiles_all += std::max<uint32_t> ( 1, ( groups + kDPThreads * t.W - 1 ) / ( kDPThreads * t.W ) );
+    }
+    const uint64_t target = ( uint64_t ) c->num_sms * 24;
+    const uint32_t want_chunks = ( uint32_t ) std::max<uint64_t> ( 1, ( target + tiles_all - 1 ) / tiles_all );
+    const size_t descb = ( ( size_t ) n * sizeof ( MiniJob ) + 255 ) & ~( size_t ) 255, resb = ( size_t ) n * 16;
+    MTX_TRY ( alloc_pinned ( &c->mpinned, &c->mpinned_cap, descb + resb, st ) );
+    MTX_TRY ( alloc_dev ( c->mjobs, descb ) );
+    MTX_TRY ( alloc_dev ( c->mres, resb ) );
+    MiniJob * hd = static_cast<MiniJob *> ( c->mpinned );
+    uint32_t * hres = reinterpret_cast<uint32_t *> ( static_cast<uint8_t *> ( c->mpinned ) + descb );
+    MiniJob * dd = static_cast<MiniJob *> ( c->mjobs.p );
+    uint32_t * dres = static_cast<uint32_t *> ( c->mres.p );
+    for ( uint32_t i = 0; i < n; ++i )
+    {
+        Job * j = js[i];
+        const motex_params & P = j->prm;
+        const bool ed = P.d == 1;
+        j->replaying = false;
+        j->structured = j->generic = j->structN = j->structN_blk = false;
+        j->launches = 0;
+        j->exec_cells = 0;
+        j->dp_ms = 0.f;
+        j->dp_timed = false;
+        j->dp_pending = false;
+        j->nblk = ( uint32_t ) ( ( j->total + 31 ) / 32 );
+        j->stride = ( j->nblk + 1 + 31 ) & ~31u;
+        const uint32_t nchunks = std::min<uint32_t> ( { want_chunks, 32u, std::max<uint32_t> ( 1, j->nblk / ( ed ? 16 : 4 ) ) } );
+        build_chunks ( j, 0, nchunks, ed ? P.l + P.e - 1 : 0, j->chunks );
+        ChunkInfo * d_chunks;
+        MTX_TRY ( upload_chunks ( j, &d_chunks ) );
+        uint32_t tbits = 5;
+        while ( ( 1ull << tbits ) < 2ull * j->nwords ) ++tbits;
+        const uint32_t nw = std::max<uint32_t> ( 1, j->nwords );
+        MiniJob & m = hd[i];
+        m = MiniJob {};
+        m.raw = dptr<uint8_t> ( j, S_RAW );
+        m.offs = dptr<uint32_t> ( j, S_OFFS );
+        m.qok = dptr<uint8_t> ( j, S_QOK );
+        m.nseq = j->nseq;
+        m.total = ( uint32_t ) j->total;
+        m.l = P.l;
+        m.tml = j->tml;
+        m.vstart = ed ? 0 : P.l - 1;
+        m.B = ( uint32_t ) j->B;
+        m.nmin = P.n;
+        m.nmax = P.N;
+        m.n_split = j->n_split;
+        m.nblk = j->nblk;
+        m.plane_stride = j->stride;
+        m.tbits = tbits;
+        m.top_aligned = ed ? 0 : 1;
+        unsigned long long * tkey;
+        MTX_TRY ( ensure ( j, S_CODES, j->total + 64, &m.codes ) );
+        MTX_TRY ( ensure ( j, S_PLANES, ( size_t ) j->B * j->stride, &m.planes ) );
+        MTX_TRY ( ensure ( j, S_VMASK, j->nblk, &m.vmask ) );
+        MTX_TRY ( ensure ( j, S_EMASK, j->nblk, &m.emask ) );
+        MTX_TRY ( ensure ( j, S_KEY0, ( size_t ) 2 << tbits, reinterpret_cast<uint32_t **> ( &tkey ) ) );
+        m.tkey = tkey;
+        MTX_TRY ( ensure ( j, S_IDX1, ( size_t ) 1 << tbits, &m.tpos ) );
+        MTX_TRY ( ensure ( j, S_UNIQ, nw, &m.uniq ) );
+        MTX_TRY ( ensure ( j, S_WPL32, ( size_t ) j->B * nw, &m.wpl ) );
+        MTX_TRY ( ensure ( j, S_UACC, nw, &m.u_acc ) );
+        MTX_TRY ( ensure ( j, S_VACC, nw, &m.v_acc ) );
+        MTX_TRY ( ensure ( j, S_FLAGS, ( size_t ) std::max<uint32_t> ( 1, j->n_split ) * nw, &m.flags ) );
+        MTX_TRY ( ensure ( j, S_MARK, j->total, &m.mark ) );
+        MTX_TRY ( ensure ( j, S_RECU, j->total, &m.rec_u ) );
+        MTX_TRY ( ensure ( j, S_RECV, j->total, &m.rec_v ) );
+        MTX_TRY ( ensure ( j, S_RECS, ( size_t ) 3 * nw, &m.recs ) );
+        m.result = dres + 4 * i;
+        memcpy ( m.cmap, pin<uint8_t> ( j, kPinCmap ), 256 );
+        pin<uint32_t> ( j, kPinScalar )[3] = 0;                     // no staging wait in this pipeline
+    }
+    MTX_CUDA ( cudaMemcpyAsync ( dd, hd, ( size_t ) n * sizeof ( MiniJob ), cudaMemcpyHostToDevice, st ) );
+    for ( Job * j : js ) MTX_TRY ( record ( j, j->ev0 ) );
+    k_mini_prep<<<n, kMiniThreads, 0, st>>> ( dd );
+    c->launches++;
+    for ( Job * j : js ) j->launches++;
+    if ( cudaError_t e = cudaGetLastError () ) return fail ( MOTEX_ECUDA, "launch of k_mini_prep failed: %s", cudaGetErrorString ( e ) );
+    MTX_CUDA ( cudaMemcpyAsync ( hres, dres, resb, cudaMemcpyDeviceToHost, st ) );
+    MTX_TRY ( sync ( c ) );
+
+    // the DP of every job with factors
+    for ( uint32_t i = 0; i < n; ++i )
+    {
+        Job * j = js[i];
+        const motex_params & P = j->prm;
+        const bool ed = P.d == 1;
+        const uint32_t U = hres[4 * i + 1];
+        j->U = U;
+        j->uniq = dptr<uint32_t> ( j, S_UNIQ );
+        if ( U == 0 ) continue;
+        j->tune = choose_tune ( j, U, ed, false );
+        DPTune cached;
+        if ( ! getenv ( "MOTEX_DP_W" ) && ! getenv ( "MOTEX_DP_UR" ) && ! getenv ( "MOTEX_DP_SWAR" ) &&
+             tune_lookup ( TuneKey { j->B, P.l, P.e, P.d }, &cached ) )
+            j->tune = cached;
+        const uint32_t groups = ( U + j->tune.NL - 1 ) / j->tune.NL;
+        j->ntiles = ( groups + kDPThreads * j->tune.W - 1 ) / ( kDPThreads * j->tune.W );
+        DPArgs & da = j->da;
+        da = DPArgs {};
+        da.text.planes = dptr<uint32_t> ( j, S_PLANES );
+        da.text.plane_stride = j->stride;
+        da.text.vmask = dptr<uint32_t> ( j, S_VMASK );
+        da.text.emask = dptr<uint32_t> ( j, S_EMASK );
+        da.text.nblk = j->nblk;
+        da.wplanes32 = dptr<uint32_t> ( j, S_WPL32 );
+        da.U = U;
+        da.l = P.l;
+        da.e = P.e;
+        da.one = 1u;
+        da.two = 2u;
+        da.neg1 = ~0u;
+        da.chunks = dptr<ChunkInfo> ( j, S_CHUNKS );
+        da.u_acc = dptr<uint32_t> ( j, S_UACC );
+        da.v_acc = dptr<uint32_t> ( j, S_VACC );
+        da.split_flags = dptr<uint8_t> ( j, S_FLAGS );
+        for ( auto & ch : j->chunks ) j->exec_cells += ( uint64_t ) U * ( ch.end - ch.warm ) * 32;
+        j->dp_pending = true;
+    }
+    if ( n == 1 ) MTX_TRY ( stage_dp ( js[0] ) );
+    else MTX_TRY ( batch_dp ( c, js, dp_ms ) );
+
+    k_mini_post<<<n, kMiniThreads, 0, st>>> ( dd );
+    c->launches++;
+    for ( Job * j : js ) j->launches++;
+    if ( cudaError_t e = cudaGetLastError () ) return fail ( MOTEX_ECUDA, "launch of k_mini_post failed: %s", cudaGetErrorString ( e ) );
+    for ( Job * j : js ) MTX_TRY ( record ( j, j->ev1 ) );
+    MTX_CUDA ( cudaMemcpyAsync ( hres, dres, resb, cudaMemcpyDeviceToHost, st ) );
+    MTX_TRY ( sync ( c ) );
+    for ( uint32_t i = 0; i < n; ++i ) js[i]->nrec = hres[4 * i + 2];
+    for ( Job * j : js ) MTX_TRY ( fetch_issue ( j ) );
+    MTX_TRY ( sync ( c ) );
+    return MOTEX_OK;
+}
+
 int ensure_pool ( motex_ctx * c, uint32_t n )
 {
     while ( c->pool.size () < n )
@@ -1589,9 +1794,10 @@ int motex_ctx_destroy ( motex_ctx * c )
     if ( ! c ) return MOTEX_OK;
     cudaSetDevice ( c->device );
     if ( c->st ) cudaStreamSynchronize ( c->st );
-    for ( DevBuf * b : { &c->bjobs, &c->bitems, &c->bcounter } )
+    for ( DevBuf * b : { &c->bjobs, &c->bitems, &c->bcounter, &c->mjobs, &c->mres } )
         if ( b->p ) cudaFree ( b->p );
     if ( c->bpinned ) cudaFreeHost ( c->bpinned );
+    if ( c->mpinned ) cudaFreeHost ( c->mpinned );
     if ( c->evb0 ) cudaEventDestroy ( c->evb0 );
     if ( c->evb1 ) cudaEventDestroy ( c->evb1 );
     cudaStream_t st = c->st;
@@ -1633,6 +1839,18 @@ int motex_gpu_run ( motex_ctx * c, const motex_params * prm, const char * const 
     if ( ! c || ! out ) return fail ( MOTEX_EINVAL, "null argument" );
     memset ( out, 0, sizeof *out );
     MTX_TRY ( motex_gpu_load ( c, prm, seqs, lens, nseq ) );
+    Job * j = &c->main;
+    if ( mini_eligible ( j ) )
+    {
+        // small input: the two-kernel pipeline around the DP
+        std::vector<Job *> one { j };
+        float dp_ms;
+        MTX_TRY ( run_mini ( c, one, &dp_ms ) );
+        MTX_TRY ( read_times ( j ) );
+        j->executed = true;
+        drop_graph ( j );                              // a later execute replays the staged pipeline
+        return fetch_build ( j, out );
+    }
     MTX_TRY ( motex_gpu_execute ( c ) );
     return motex_gpu_fetch ( c, out );
 }
@@ -1644,14 +1862,33 @@ int motex_gpu_run_batch ( motex_ctx * c, const motex_job * jobs, uint32_t njobs,
     if ( njobs == 0 ) return MOTEX_OK;
     MTX_CUDA ( cudaSetDevice ( c->device ) );
     MTX_TRY ( ensure_pool ( c, njobs ) );
-    std::vector<Job *> js ( njobs );
+    std::vector<Job *> all ( njobs ), js, mini;
+    std::vector<uint32_t> js_idx, mini_idx;
     for ( uint32_t i = 0; i < njobs; ++i )
     {
-        js[i] = c->pool[i].get ();
-        js[i]->replaying = false;
-        js[i]->batched = true;
-        MTX_TRY ( load_job ( js[i], jobs[i].prm, jobs[i].seqs, jobs[i].lens, jobs[i].nseq, 0, true ) );
+        all[i] = c->pool[i].get ();
+        all[i]->replaying = false;
+        all[i]->batched = true;
+        MTX_TRY ( load_job ( all[i], jobs[i].prm, jobs[i].seqs, jobs[i].lens, jobs[i].nseq, 0, true ) );
+        if ( mini_eligible ( all[i] ) ) { mini.push_back ( all[i] ); mini_idx.push_back ( i ); }
+        else { js.push_back ( all[i] ); js_idx.push_back ( i ); }
     }
+    // small jobs: the two-kernel pipeline, one launch per stage for all of them
+    if ( ! mini.empty () )
+    {
+        float mini_dp = 0.f;
+        MTX_TRY ( run_mini ( c, mini, &mini_dp ) );
+        for ( uint32_t k = 0; k < mini.size (); ++k )
+        {
+            Job * j = mini[k];
+            MTX_TRY ( read_times ( j ) );
+            if ( mini.size () > 1 ) j->dp_ms = mini_dp;     // the batch shares its DP launches
+            j->executed = true;
+            MTX_TRY ( fetch_build ( j, &results[mini_idx[k]] ) );
+        }
+    }
+    if ( js.empty () ) return MOTEX_OK;
+    njobs = ( uint32_t ) js.size ();
     for ( Job * j : js ) MTX_TRY ( stage_presence ( j ) );
     MTX_TRY ( sync ( c ) );
     std::vector<char> sorted ( njobs );
@@ -1681,7 +1918,7 @@ int motex_gpu_run_batch ( motex_ctx * c, const motex_job * jobs, uint32_t njobs,
         MTX_TRY ( read_times ( js[i] ) );
         js[i]->dp_ms = dp_ms;                        // the batch shares its DP launches
         js[i]->executed = true;
-        MTX_TRY ( fetch_records ( js[i], &results[i] ) );
+        MTX_TRY ( fetch_records ( js[i], &results[js_idx[i]] ) );
     }
     return MOTEX_OK;
 }

@@ -245,10 +245,19 @@ struct MiniJob
     uint32_t *           rec_v;
     uint32_t *           recs;           // 3 words per motif
     uint32_t *           result;
+    uint32_t *           part;           // marks per CTA share (ctas words)
+    uint32_t             nwords;         // factors (bound of the distinct count)
+    uint32_t             ctas;           // CTAs of this job (<= the grid's x)
     uint8_t              cmap[256];
 };
-__global__ void k_mini_prep ( const MiniJob * jobs );
-__global__ void k_mini_post ( const MiniJob * jobs );
+constexpr uint32_t kMiniMaxCtas = 16;
+__global__ void k_mini_clear ( const MiniJob * jobs );
+__global__ void k_mini_pack ( const MiniJob * jobs );
+__global__ void k_mini_uniq ( const MiniJob * jobs );
+__global__ void k_mini_planes ( const MiniJob * jobs );
+__global__ void k_mini_final ( const MiniJob * jobs );
+__global__ void k_mini_count ( const MiniJob * jobs );
+__global__ void k_mini_write ( const MiniJob * jobs );
 
 // One job of a batched launch and one unit of its work.
 struct JobDesc

@@ -156,7 +156,7 @@ struct motex_ctx
     DevBuf bjobs, bitems, bcounter;
     void * bpinned = nullptr;
     size_t bpinned_cap = 0;
-    DevBuf mjobs, mres;                        // small-job pipeline: descriptors, result words
+    DevBuf mjobs, mres, mpart;                 // small-job pipeline: descriptors, result words, shares
     void * mpinned = nullptr;
     size_t mpinned_cap = 0;
     cudaEvent_t evb0 = nullptr, evb1 = nullptr;
@@ -1587,11 +1587,11 @@ bool mini_eligible ( Job * j )
 }
 
 /*
- * The small-job pipeline for loaded, eligible jobs: k_mini_prep (one CTA per
- * job) -> sync (distinct-factor counts) -> the DP (the job's static launch
- * when alone, the batch's persistent launches otherwise) -> k_mini_post ->
- * sync (motif counts) -> record copies queued -> sync.  The caller reads the
- * times and builds the results.
+ * The small-job pipeline for loaded, eligible jobs: clear, pack, uniq,
+ * planes (grids of every job's CTAs) -> sync (distinct-factor counts) -> the
+ * DP (the job's static launch when alone, the batch's persistent launches
+ * otherwise) -> final, count, write -> sync (motif counts) -> record copies
+ * queued -> sync.  The caller reads the times and builds the results.
  */
 int run_mini ( motex_ctx * c, std::vector<Job *> & js, float * dp_ms )
 {
@@ -1613,6 +1613,8 @@ int run_mini ( motex_ctx * c, std::vector<Job *> & js, float * dp_ms )
     MTX_TRY ( alloc_pinned ( &c->mpinned, &c->mpinned_cap, descb + resb, st ) );
     MTX_TRY ( alloc_dev ( c->mjobs, descb ) );
     MTX_TRY ( alloc_dev ( c->mres, resb ) );
+    MTX_TRY ( alloc_dev ( c->mpart, ( size_t ) n * kMiniMaxCtas * sizeof ( uint32_t ) ) );
+    uint32_t max_ctas = 1;
     MiniJob * hd = static_cast<MiniJob *> ( c->mpinned );
     uint32_t * hres = reinterpret_cast<uint32_t *> ( static_cast<uint8_t *> ( c->mpinned ) + descb );
     MiniJob * dd = static_cast<MiniJob *> ( c->mjobs.p );
@@ -1674,17 +1676,33 @@ int run_mini ( motex_ctx * c, std::vector<Job *> & js, float * dp_ms )
         MTX_TRY ( ensure ( j, S_RECV, j->total, &m.rec_v ) );
         MTX_TRY ( ensure ( j, S_RECS, ( size_t ) 3 * nw, &m.recs ) );
         m.result = dres + 4 * i;
+        m.part = static_cast<uint32_t *> ( c->mpart.p ) + ( size_t ) i * kMiniMaxCtas;
+        m.nwords = j->nwords;
+        // a CTA per 4096 symbols, at most kMiniMaxCtas
+        m.ctas = ( uint32_t ) std::min<uint64_t> ( kMiniMaxCtas, std::max<uint64_t> ( 1, ( j->total + 4095 ) / 4096 ) );
+        max_ctas = std::max ( max_ctas, m.ctas );
         memcpy ( m.cmap, pin<uint8_t> ( j, kPinCmap ), 256 );
         pin<uint32_t> ( j, kPinScalar )[3] = 0;                     // no staging wait in this pipeline
     }
     MTX_CUDA ( cudaMemcpyAsync ( dd, hd, ( size_t ) n * sizeof ( MiniJob ), cudaMemcpyHostToDevice, st ) );
+    MTX_CUDA ( cudaMemsetAsync ( dres, 0, resb, st ) );
     for ( Job * j : js ) MTX_TRY ( record ( j, j->ev0 ) );
-    k_mini_prep<<<n, kMiniThreads, 0, st>>> ( dd );
-    c->launches++;
-    for ( Job * j : js ) j->launches++;
-    if ( cudaError_t e = cudaGetLastError () ) return fail ( MOTEX_ECUDA, "launch of k_mini_prep failed: %s", cudaGetErrorString ( e ) );
+    const dim3 grid ( max_ctas, n );
+    auto launch = [&] ( void ( *k ) ( const MiniJob * ), const char * name ) -> int {
+        k<<<grid, kMiniThreads, 0, st>>> ( dd );
+        c->launches++;
+        for ( Job * j : js ) j->launches++;
+        if ( cudaError_t e = cudaGetLastError () ) return fail ( MOTEX_ECUDA, "launch of %s failed: %s", name, cudaGetErrorString ( e ) );
+        return MOTEX_OK;
+    };
+    MTX_TRY ( launch ( k_mini_clear, "k_mini_clear" ) );
+    MTX_TRY ( launch ( k_mini_pack, "k_mini_pack" ) );
+    MTX_TRY ( launch ( k_mini_uniq, "k_mini_uniq" ) );
+    MTX_TRY ( launch ( k_mini_planes, "k_mini_planes" ) );
     MTX_CUDA ( cudaMemcpyAsync ( hres, dres, resb, cudaMemcpyDeviceToHost, st ) );
     MTX_TRY ( sync ( c ) );
+    for ( uint32_t i = 0; i < n; ++i )
+        if ( hres[4 * i] ) return fail ( MOTEX_ECUDA, "small-job pipeline: factor table overflow" );
 
     // the DP of every job with factors
     for ( uint32_t i = 0; i < n; ++i )
@@ -1727,10 +1745,9 @@ int run_mini ( motex_ctx * c, std::vector<Job *> & js, float * dp_ms )
     if ( n == 1 ) MTX_TRY ( stage_dp ( js[0] ) );
     else MTX_TRY ( batch_dp ( c, js, dp_ms ) );
 
-    k_mini_post<<<n, kMiniThreads, 0, st>>> ( dd );
-    c->launches++;
-    for ( Job * j : js ) j->launches++;
-    if ( cudaError_t e = cudaGetLastError () ) return fail ( MOTEX_ECUDA, "launch of k_mini_post failed: %s", cudaGetErrorString ( e ) );
+    MTX_TRY ( launch ( k_mini_final, "k_mini_final" ) );
+    MTX_TRY ( launch ( k_mini_count, "k_mini_count" ) );
+    MTX_TRY ( launch ( k_mini_write, "k_mini_write" ) );
     for ( Job * j : js ) MTX_TRY ( record ( j, j->ev1 ) );
     MTX_CUDA ( cudaMemcpyAsync ( hres, dres, resb, cudaMemcpyDeviceToHost, st ) );
     MTX_TRY ( sync ( c ) );
@@ -1794,7 +1811,7 @@ int motex_ctx_destroy ( motex_ctx * c )
     if ( ! c ) return MOTEX_OK;
     cudaSetDevice ( c->device );
     if ( c->st ) cudaStreamSynchronize ( c->st );
-    for ( DevBuf * b : { &c->bjobs, &c->bitems, &c->bcounter, &c->mjobs, &c->mres } )
+    for ( DevBuf * b : { &c->bjobs, &c->bitems, &c->bcounter, &c->mjobs, &c->mres, &c->mpart } )
         if ( b->p ) cudaFree ( b->p );
     if ( c->bpinned ) cudaFreeHost ( c->bpinned );
     if ( c->mpinned ) cudaFreeHost ( c->mpinned );

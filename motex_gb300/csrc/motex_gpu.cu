@@ -414,8 +414,9 @@ DPTune choose_tune ( Job * j, uint32_t U, bool ed, bool generic )
  * chunks as fill every SM's CTA slots several times, like the real grid, and
  * long enough that the per-CTA set-up weighs as little as in the real run;
  * time per cell from CUDA events picks the winner; accumulators are cleared
- * afterwards.  A batched job's entry also picks the shape of the
- * persistent kernel its class runs (where one implements it).  Entries are shared by every context of the
+ * afterwards.  Batched jobs do not tune (their probes would stall the
+ * batch); a key's entry also picks the shape of the persistent kernel its
+ * class runs (where one implements it).  Entries are shared by every context of the
  * process and, with MOTEX_TUNE_CACHE=<file>, read from and appended to that
  * file.  MOTEX_AUTOTUNE=0 turns tuning off (the defaults of choose_tune
  * apply); explicit MOTEX_DP_* overrides win over both.
@@ -770,8 +771,9 @@ int stage_plan ( Job * j, bool sorted )
     da.neg1 = ~0u;
     if ( ! j->replaying ) j->tune = choose_tune ( j, U, ed, j->generic );
     bool tune_now = false;
-    // batched jobs tune too: the key's entry then also picks the persistent
-    // kernel's shape (batch_dp)
+    // a batched job takes the key's entry when there is one but does not
+    // tune: the probes would stall its batch-mates (a serving batch above
+    // all); batch_dp picks the persistent kernel's shape from the entry
     if ( ! j->replaying && ! j->generic && ! getenv ( "MOTEX_DP_W" ) && ! getenv ( "MOTEX_DP_UR" ) &&
          ! getenv ( "MOTEX_DP_SWAR" ) )
     {
@@ -779,7 +781,7 @@ int stage_plan ( Job * j, bool sorted )
         const bool enabled = ! ( at && atoi ( at ) == 0 );
         DPTune cached;
         if ( enabled && tune_lookup ( TuneKey { B, P.l, P.e, P.d }, &cached ) ) j->tune = cached;
-        else tune_now = enabled && ( uint64_t ) U * j->total >= kTuneMinCells;
+        else tune_now = enabled && ! j->batched && ( uint64_t ) U * j->total >= kTuneMinCells;
     }
     const DPTune & tune = j->tune;
     const uint32_t groups = ( U + tune.NL - 1 ) / tune.NL;        // factors per register: NL
@@ -1489,6 +1491,19 @@ int batch_dp ( motex_ctx * c, std::vector<Job *> & jobs, float * dp_ms )
         const uint32_t groups = ( j->U + j->tune.NL - 1 ) / j->tune.NL;
         j->ntiles = ( groups + kDPThreads * j->tune.W - 1 ) / ( kDPThreads * j->tune.W );
         classes[k].push_back ( j );
+    }
+    // a class of one job runs that job's static grid: one launch over its
+    // (tile, chunk) items either way, and the one-job kernel holds the job's
+    // constants in the constant bank (measured on the 2000-protein edit-
+    // distance set: 294 ms static against 315-328 ms persistent)
+    for ( auto it = classes.begin (); it != classes.end (); )
+    {
+        if ( it->second.size () == 1 )
+        {
+            MTX_TRY ( stage_dp ( it->second[0] ) );
+            it = classes.erase ( it );
+        }
+        else ++it;
     }
     size_t njobs = 0, nitems = 0;
     for ( auto & kv : classes )

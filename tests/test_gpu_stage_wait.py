@@ -26,6 +26,8 @@ def test_staging_wait_gives_up_then_context_recovers(native_built, oracle_port, 
     wl = W.dna_ed(seed=11, scale=0.05, d=d)            # 60 sequences, several staged tiles per CTA
     wl.k, wl.e, wl.q = 10, 1, 10
     prm = native_built.make_params(d, wl.k, wl.e, wl.q)
+    # the staged pipeline (the small-job pipeline packs without TMA staging)
+    monkeypatch.setenv("MOTEX_MINI", "0")
     ctx = native_built.Context(0)
     try:
         monkeypatch.setenv("MOTEX_PACK_WAIT_POLLS", "0")

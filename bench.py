@@ -238,6 +238,18 @@ def traffic_record(workload):
         return None
 
 
+def executed_record(workload):
+    """Executed-instruction figures of the workload's DP kernel from the
+    committed one-kernel ncu summary (profiles/dp_executed.json), if any:
+    thread instructions per algorithmic cell and the pipes' utilisation of
+    one captured launch.  Unlike roofline.frac, these are utilisations (<= 1)."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "dp_executed.json")) as f:
+            return json.load(f).get(workload)
+    except (OSError, ValueError):
+        return None
+
+
 def aggregate_replicas(step_s, e2e_s, cells, world):
     """Whole-job figures over `world` replicas: the slowest rank's times (max
     over ranks, host all-reduce) and the work of all ranks.  Returns
@@ -536,6 +548,12 @@ def run_gpu(args, rank, world, local_rank):
     achieved = alg_ops / dp_s / 1e12 if dp_s > 0 else 0.0
     tr = traffic_record(args.workload)
     kernel = dp_kernel_name(wl)
+    if not wl.boxes and wl.k <= 32:
+        # the launch shape the autotuner settled on for this key, if it tuned
+        sigma = len(set("".join(wl.seqs)))
+        shape = native.tune_lookup(max(2, (sigma - 1).bit_length()), wl.k, wl.e, wl.d)
+        if shape:
+            kernel += " W=%d NL=%d UR=%d" % shape
     roofline = {"bound": "int32_alu", "kernel": kernel, "achieved": round(achieved, 3),
                 "peak": round(iadd, 3), "unit": "Tops/s", "frac": round(achieved / iadd, 4) if iadd else None,
                 "peak_source": "measured int32 add throughput, all pipes (motex_probe_int_peak), same run",
@@ -544,7 +562,10 @@ def run_gpu(args, rank, world, local_rank):
                 "dp_ms": round(dp_s * 1e3, 3), "dp_cells_per_s": round(first.unique_words * total_pos / dp_s, 1),
                 "traffic": tr,
                 "note": "algorithmic ops per cell; SWAR lanes (2-4 cells per instruction) and the shared Eq "
-                        "table execute fewer, so frac can exceed 1"}
+                        "table execute fewer, so frac can exceed 1; `executed` gives the measured utilisations"}
+    ex = executed_record(args.workload)
+    if ex:
+        roofline["executed"] = ex
     if wl.d == 0 and not wl.boxes and dp_s > 0 and popc:
         # plain Hamming runs one population count per cell: its second roof
         popc_rate = first.unique_words * total_pos / dp_s / 1e12

@@ -63,7 +63,7 @@ __global__ void __launch_bounds__ ( kDPThreads ) k_dp_structN_blk ( const Struct
     uint32_t * ring = ring_all + ( size_t ) warp * nslot * NR * 32;   // [slot][row][lane]
     uint32_t * s_eq = ring_all + ( size_t ) NWARP * nslot * NR * 32;  // [code][thread]
     __shared__ uint32_t s_row[NWARP][2][32];                    // edit distance: Eq-table offsets of a block
-    __shared__ uint32_t s_win[2][32 * B];                       // Hamming: replicated windows of a block
+    __shared__ uint32_t s_win[NWARP][2][32 * B];                // Hamming: replicated windows of a block, per warp
     __shared__ uint32_t s_fit[NWARP][32];                       // chain-fit masks by last-box offset
 
     for ( uint32_t i = threadIdx.x; i < NS * NGAP; i += kDPThreads )
@@ -145,6 +145,15 @@ __global__ void __launch_bounds__ ( kDPThreads ) k_dp_structN_blk ( const Struct
 
     // occurrences of the chains starting at the positions `h` of block E
     auto count = [&] ( uint32_t E, uint32_t h ) {
+        // cheap exit: none of the box-1 rows this lane's structures reach
+        // hits in the blocks where box 1 of a chain starting in E can end
+        {
+            uint32_t any1 = 0;
+            const uint32_t qa = E + ( C.lo[0] >> 5 ), qb = E + ( ( C.lo[0] + C.D[0] + 30 ) >> 5 );
+            for ( uint32_t q = qa; q <= qb; ++q )
+                for ( uint32_t o = 0; o < C.D[0]; ++o ) any1 |= ring[( ( q % nslot ) * NR + 1 ) * 32 + lane + o];
+            if ( ! any1 ) return;
+        }
         const uint32_t * fit = s_fit[warp];
         for ( uint32_t kk = kvalid; kk; kk &= kk - 1 )
         {
@@ -236,17 +245,19 @@ __global__ void __launch_bounds__ ( kDPThreads ) k_dp_structN_blk ( const Struct
             }
             else
             {
-                // the replicated windows are the same for every thread: built
-                // once per block into shared memory (double-buffered)
-                uint32_t * wsm = s_win[par];
-                for ( uint32_t i = threadIdx.x; i < 32u * B; i += kDPThreads )
+                // the replicated windows are the same for every thread: each
+                // warp builds the block's once into its own double-buffered
+                // rows (lane r takes position r) -- a warp barrier, where a
+                // CTA-wide buffer made the CTA barrier the top stall
+                uint32_t * wsm = s_win[warp][par];
+#pragma unroll
+                for ( int pl = 0; pl < B; ++pl )
                 {
-                    const uint32_t pl = i >> 5, r = i & 31u;
                     const uint32_t pw = __ldg ( planes + ( size_t ) pl * stride + kb );
                     const uint32_t cw = __ldg ( planes + ( size_t ) pl * stride + kb + 1 );
-                    wsm[i] = ( __funnelshift_rc ( pw, cw, r + 1 ) >> ( 32 - C.Lmax ) ) * C.rep;
+                    wsm[pl * 32 + lane] = ( __funnelshift_rc ( pw, cw, lane + 1 ) >> ( 32 - C.Lmax ) ) * C.rep;
                 }
-                __syncthreads ();
+                __syncwarp ();
 #pragma unroll 8
                 for ( int r = 0; r < 32; ++r )
                 {

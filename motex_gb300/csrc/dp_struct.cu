@@ -912,7 +912,9 @@ __global__ void k_struct_finalize ( StructFinalizeArgs a )
 // checked directly at that end position: Hamming compares one window of the
 // text bit planes with the box factor's planes; edit distance reruns the
 // Myers column over the last l_b + e_b text symbols (a restart that far back
-// is exact for the <= e_b test) or from the sequence start.
+// is exact for the <= e_b test) or from the sequence start.  Word is the
+// row width: 32-bit rows for boxes of at most 32 symbols, 64-bit rows
+// (wpl64) when a box is longer, up to 64.
 
 namespace mtx
 {
@@ -920,60 +922,102 @@ namespace mtx
 namespace
 {
 
-template <int B>
-__device__ __forceinline__ void text_window ( const TextView & tv, uint32_t p, uint32_t ( &Y )[B] )
+template <typename Word>
+struct WordBits;
+template <>
+struct WordBits<uint32_t>
 {
-    // 32 symbols ending at p (p at bit 31)
+    static constexpr uint32_t value = 32;
+    __device__ static uint32_t popc ( uint32_t x ) { return __popc ( x ); }
+};
+template <>
+struct WordBits<unsigned long long>
+{
+    static constexpr uint32_t value = 64;
+    __device__ static uint32_t popc ( unsigned long long x ) { return __popcll ( x ); }
+};
+
+// The window of text symbols ending at position p, p at the top bit, from
+// the plane words of the blocks (word k + 1 of a plane holds block k).
+template <int B, typename Word>
+__device__ __forceinline__ void text_window ( const TextView & tv, uint32_t p, Word ( &Y )[B] )
+{
     const uint32_t blk = p >> 5, r = p & 31u;
 #pragma unroll
     for ( int b = 0; b < B; ++b )
     {
-        const uint32_t lo = __ldg ( tv.planes + ( size_t ) b * tv.plane_stride + blk );
-        const uint32_t hi = __ldg ( tv.planes + ( size_t ) b * tv.plane_stride + blk + 1 );
-        Y[b] = __funnelshift_rc ( lo, hi, r + 1 );
+        const uint32_t * pl = tv.planes + ( size_t ) b * tv.plane_stride;
+        const uint32_t cur = __ldg ( pl + blk + 1 ), prev = __ldg ( pl + blk );
+        if constexpr ( WordBits<Word>::value == 32 )
+            Y[b] = __funnelshift_rc ( prev, cur, r + 1 );
+        else
+        {
+            const unsigned long long pp = blk >= 1 ? __ldg ( pl + blk - 1 ) : 0u;
+            const unsigned long long lo = ( ( unsigned long long ) prev << 32 ) | pp;
+            Y[b] = ( lo >> ( r + 1 ) ) | ( ( unsigned long long ) cur << ( 63 - r ) );
+        }
     }
 }
 
-template <int B, bool ED>
+template <typename Word>
+__device__ __forceinline__ Word top_mask ( uint32_t l )
+{
+    constexpr uint32_t BITS = WordBits<Word>::value;
+    return l >= BITS ? ~( Word ) 0 : ~( ( ( Word ) 1 << ( BITS - l ) ) - 1 );
+}
+
+// Box planes of the factor ending at pattern position q.
+template <int B, typename Word>
+__device__ __forceinline__ void box_planes ( const StructNArgs & a, int box, uint32_t q, Word ( &w )[B] )
+{
+#pragma unroll
+    for ( int b = 0; b < B; ++b )
+    {
+        if constexpr ( WordBits<Word>::value == 32 )
+            w[b] = __ldg ( a.wpl + ( ( size_t ) box * B + b ) * a.total + q );
+        else
+            w[b] = __ldg ( a.wpl64 + ( ( size_t ) box * B + b ) * a.total + q );
+    }
+}
+
+template <int B, bool ED, typename Word>
 __device__ bool box_hit ( const StructNArgs & a, int box, uint32_t q, uint32_t p, uint32_t tstart )
 {
     const uint32_t lb = a.blen[box], eb = a.berr[box];
-    const uint32_t * __restrict__ wpl = a.wpl + ( size_t ) box * B * a.total;
-    uint32_t w[B];
-#pragma unroll
-    for ( int b = 0; b < B; ++b ) w[b] = __ldg ( wpl + ( size_t ) b * a.total + q );
+    Word w[B];
+    box_planes<B, Word> ( a, box, q, w );
     if constexpr ( ! ED )
     {
-        uint32_t Y[B];
-        text_window<B> ( a.text, p, Y );
-        const uint32_t top = lb >= 32 ? 0xffffffffu : ~( ( 1u << ( 32 - lb ) ) - 1u );
-        uint32_t x = w[0] ^ Y[0];
+        Word Y[B];
+        text_window<B, Word> ( a.text, p, Y );
+        Word x = w[0] ^ Y[0];
 #pragma unroll
         for ( int b = 1; b < B; ++b ) x |= w[b] ^ Y[b];
-        return __popc ( x & top ) <= eb;
+        return WordBits<Word>::popc ( x & top_mask<Word> ( lb ) ) <= eb;
     }
     else
     {
         const uint32_t back = lb + eb - 1;
         const uint32_t s0 = ( p >= tstart + back ) ? p - back : tstart;
-        uint32_t Pv = ~0u, Mv = 0, sc = lb;
+        Word Pv = ~( Word ) 0, Mv = 0;
+        uint32_t sc = lb;
         const uint32_t sh = lb - 1;
         for ( uint32_t r = s0; r <= p; ++r )
         {
             const uint32_t blk = ( r >> 5 ) + 1, bit = r & 31u;
-            uint32_t x = 0;
+            Word x = 0;
 #pragma unroll
             for ( int b = 0; b < B; ++b )
             {
-                const uint32_t T = 0u - ( ( __ldg ( a.text.planes + ( size_t ) b * a.text.plane_stride + blk ) >> bit ) & 1u );
+                const Word T = ( Word ) 0 - ( Word ) ( ( __ldg ( a.text.planes + ( size_t ) b * a.text.plane_stride + blk ) >> bit ) & 1u );
                 x |= w[b] ^ T;
             }
-            const uint32_t Eq = ~x;
-            const uint32_t Xv = Eq | Mv;
-            const uint32_t Xh = ( ( ( Eq & Pv ) + Pv ) ^ Pv ) | Eq;
-            uint32_t Ph = Mv | ~( Xh | Pv );
-            uint32_t Mh = Pv & Xh;
-            sc += ( ( Ph >> sh ) & 1u ) - ( ( Mh >> sh ) & 1u );
+            const Word Eq = ~x;
+            const Word Xv = Eq | Mv;
+            const Word Xh = ( ( ( Eq & Pv ) + Pv ) ^ Pv ) | Eq;
+            Word Ph = Mv | ~( Xh | Pv );
+            Word Mh = Pv & Xh;
+            sc += ( uint32_t ) ( ( Ph >> sh ) & 1u ) - ( uint32_t ) ( ( Mh >> sh ) & 1u );
             Ph <<= 1;
             Mh <<= 1;
             Pv = Mh | ~( Xv | Ph );
@@ -985,7 +1029,7 @@ __device__ bool box_hit ( const StructNArgs & a, int box, uint32_t q, uint32_t p
 
 } // namespace
 
-template <int B, bool ED>
+template <int B, bool ED, typename Word>
 __global__ void __launch_bounds__ ( kDPThreads ) k_dp_structN ( const StructNArgs a )
 {
     extern __shared__ uint32_t smem[];
@@ -1001,19 +1045,27 @@ __global__ void __launch_bounds__ ( kDPThreads ) k_dp_structN ( const StructNArg
     const uint32_t jx = blockIdx.x * kDPThreads + threadIdx.x;
     const bool row = jx < a.total && a.row_ok[jx];
     const uint32_t xend = jx < a.total ? a.row_end[jx] : 0;
-    uint32_t w0[B];
+    Word w0[B];
+    if ( jx < a.total ) box_planes<B, Word> ( a, 0, jx, w0 );
+    else
 #pragma unroll
-    for ( int b = 0; b < B; ++b ) w0[b] = jx < a.total ? a.wpl[( size_t ) b * a.total + jx] : 0u;
+        for ( int b = 0; b < B; ++b ) w0[b] = 0;
     const uint32_t l0 = a.l0;
-    const uint32_t top0 = l0 >= 32 ? 0xffffffffu : ~( ( 1u << ( 32 - l0 ) ) - 1u );
+    const Word top0 = top_mask<Word> ( l0 );
     const ChunkInfo ch = a.chunks[blockIdx.y];
     int cur_split = ch.first_split;
-    uint32_t Pv = ~0u, Mv = 0, sc = l0;
+    Word Pv = ~( Word ) 0, Mv = 0;
+    uint32_t sc = l0;
     uint32_t tstart = 0;                                            // start of the current text sequence
     bool tstart_known = false;
-    uint32_t prev[B];
+    // plane words of the two blocks before the current one (Hamming windows)
+    uint32_t prev[B], pp[B];
 #pragma unroll
-    for ( int b = 0; b < B; ++b ) prev[b] = __ldg ( a.text.planes + ( size_t ) b * a.text.plane_stride + ch.warm );
+    for ( int b = 0; b < B; ++b )
+    {
+        prev[b] = __ldg ( a.text.planes + ( size_t ) b * a.text.plane_stride + ch.warm );
+        pp[b] = ch.warm >= 1 ? __ldg ( a.text.planes + ( size_t ) b * a.text.plane_stride + ch.warm - 1 ) : 0u;
+    }
 
     auto flush = [&] () {
         for ( uint32_t k = 0; k < NS; ++k )
@@ -1040,15 +1092,15 @@ __global__ void __launch_bounds__ ( kDPThreads ) k_dp_structN ( const StructNArg
             bool h0;
             if constexpr ( ED )
             {
-                uint32_t x = 0;
+                Word x = 0;
 #pragma unroll
-                for ( int b = 0; b < B; ++b ) x |= w0[b] ^ ( 0u - ( ( cur[b] >> r ) & 1u ) );
-                const uint32_t Eq = ~x;
-                const uint32_t Xv = Eq | Mv;
-                const uint32_t Xh = ( ( ( Eq & Pv ) + Pv ) ^ Pv ) | Eq;
-                uint32_t Ph = Mv | ~( Xh | Pv );
-                uint32_t Mh = Pv & Xh;
-                sc += ( ( Ph >> ( l0 - 1 ) ) & 1u ) - ( ( Mh >> ( l0 - 1 ) ) & 1u );
+                for ( int b = 0; b < B; ++b ) x |= w0[b] ^ ( ( Word ) 0 - ( Word ) ( ( cur[b] >> r ) & 1u ) );
+                const Word Eq = ~x;
+                const Word Xv = Eq | Mv;
+                const Word Xh = ( ( ( Eq & Pv ) + Pv ) ^ Pv ) | Eq;
+                Word Ph = Mv | ~( Xh | Pv );
+                Word Mh = Pv & Xh;
+                sc += ( uint32_t ) ( ( Ph >> ( l0 - 1 ) ) & 1u ) - ( uint32_t ) ( ( Mh >> ( l0 - 1 ) ) & 1u );
                 Ph <<= 1;
                 Mh <<= 1;
                 Pv = Mh | ~( Xv | Ph );
@@ -1057,10 +1109,18 @@ __global__ void __launch_bounds__ ( kDPThreads ) k_dp_structN ( const StructNArg
             }
             else
             {
-                uint32_t x = 0;
+                Word x = 0;
 #pragma unroll
-                for ( int b = 0; b < B; ++b ) x |= w0[b] ^ __funnelshift_rc ( prev[b], cur[b], r + 1 );
-                h0 = __popc ( x & top0 ) <= a.e0;
+                for ( int b = 0; b < B; ++b )
+                {
+                    Word Y;
+                    if constexpr ( WordBits<Word>::value == 32 ) Y = __funnelshift_rc ( prev[b], cur[b], r + 1 );
+                    else
+                        Y = ( ( ( ( unsigned long long ) prev[b] << 32 ) | pp[b] ) >> ( r + 1 ) ) |
+                            ( ( unsigned long long ) cur[b] << ( 63 - r ) );
+                    x |= w0[b] ^ Y;
+                }
+                h0 = WordBits<Word>::popc ( x & top0 ) <= a.e0;
             }
             if ( row && counting && h0 && ( ( vm >> r ) & 1u ) )
             {
@@ -1079,7 +1139,7 @@ __global__ void __launch_bounds__ ( kDPThreads ) k_dp_structN ( const StructNArg
                         for ( uint32_t g = 0; g < NG && ok; ++g )
                         {
                             const uint32_t q = jx + s_off[k * NG + g], p = it + s_off[l * NG + g];
-                            ok = p < tend && box_hit<B, ED> ( a, ( int ) g + 1, q, p, tstart );
+                            ok = p < tend && box_hit<B, ED, Word> ( a, ( int ) g + 1, q, p, tstart );
                         }
                         if ( ok ) s_cnt[k * kDPThreads] += 1;
                     }
@@ -1092,14 +1152,18 @@ __global__ void __launch_bounds__ ( kDPThreads ) k_dp_structN ( const StructNArg
                     flush ();
                     cur_split = -1;
                 }
-                Pv = ~0u;
+                Pv = ~( Word ) 0;
                 Mv = 0;
                 sc = l0;
                 tstart_known = false;
             }
         }
 #pragma unroll
-        for ( int b = 0; b < B; ++b ) prev[b] = cur[b];
+        for ( int b = 0; b < B; ++b )
+        {
+            pp[b] = prev[b];
+            prev[b] = cur[b];
+        }
     }
     for ( uint32_t k = 0; k < NS; ++k )
     {
@@ -1121,35 +1185,76 @@ __global__ void __launch_bounds__ ( kDPThreads ) k_dp_structN ( const StructNArg
     }
 }
 
+size_t structN_smem_bytes ( const StructNArgs & a )
+{
+    return ( ( size_t ) a.nstructs * a.ngaps + ( size_t ) 3 * a.nstructs * kDPThreads ) * sizeof ( uint32_t );
+}
+
+namespace
+{
+
+template <int B, bool ED, typename Word>
+bool launch_structN_k ( const StructNArgs & a, dim3 grid, cudaStream_t st )
+{
+    const size_t smem = structN_smem_bytes ( a );
+    if ( cudaFuncSetAttribute ( k_dp_structN<B, ED, Word>, cudaFuncAttributeMaxDynamicSharedMemorySize, ( int ) smem ) !=
+         cudaSuccess )
+        return false;
+    k_dp_structN<B, ED, Word><<<grid, kDPThreads, smem, st>>> ( a );
+    return true;
+}
+
+template <int B>
+bool launch_structN_b ( const StructNArgs & a, bool ed, bool wide, dim3 grid, cudaStream_t st )
+{
+    if ( wide )
+        return ed ? launch_structN_k<B, true, unsigned long long> ( a, grid, st )
+                  : launch_structN_k<B, false, unsigned long long> ( a, grid, st );
+    return ed ? launch_structN_k<B, true, uint32_t> ( a, grid, st ) : launch_structN_k<B, false, uint32_t> ( a, grid, st );
+}
+
+} // namespace
+
 bool launch_dp_structN ( const StructNArgs & a, int B, bool ed, dim3 grid, cudaStream_t st )
 {
-    if ( a.l0 < 1 || a.l0 > 32 || a.nstructs < 1 || a.nstructs > kMaxStructsN || a.ngaps < 1 || a.ngaps > kMaxGapsN )
-        return false;
+    if ( a.nstructs < 1 || a.nstructs > kMaxStructsN || a.ngaps < 1 || a.ngaps > kMaxGapsN ) return false;
+    if ( structN_smem_bytes ( a ) > kStructNMaxSmem ) return false;
+    uint32_t maxlen = 0;
     for ( uint32_t g = 0; g <= a.ngaps; ++g )
-        if ( a.blen[g] < 1 || a.blen[g] > 32 ) return false;
-    const size_t smem = ( ( size_t ) a.nstructs * a.ngaps + ( size_t ) 3 * a.nstructs * kDPThreads ) * sizeof ( uint32_t );
-#define MTX_SN( BB )                                                                                   \
-    case BB:                                                                                           \
-        if ( ed )                                                                                      \
-        {                                                                                              \
-            cudaFuncSetAttribute ( k_dp_structN<BB, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, ( int ) smem ); \
-            k_dp_structN<BB, true><<<grid, kDPThreads, smem, st>>> ( a );                              \
-        }                                                                                              \
-        else                                                                                           \
-        {                                                                                              \
-            cudaFuncSetAttribute ( k_dp_structN<BB, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, ( int ) smem ); \
-            k_dp_structN<BB, false><<<grid, kDPThreads, smem, st>>> ( a );                             \
-        }                                                                                              \
-        return true;
+    {
+        if ( a.blen[g] < 1 || a.blen[g] > kStructMaxBox ) return false;
+        maxlen = std::max ( maxlen, a.blen[g] );
+    }
+    const bool wide = maxlen > 32;
+    if ( wide != a.wide ) return false;                             // planes built at the other width
     switch ( B )
     {
-        MTX_SN ( 2 )
-        MTX_SN ( 3 )
-        MTX_SN ( 4 )
-        MTX_SN ( 5 )
+        case 1:
+        case 2: return launch_structN_b<2> ( a, ed, wide, grid, st );
+        case 3: return launch_structN_b<3> ( a, ed, wide, grid, st );
+        case 4: return launch_structN_b<4> ( a, ed, wide, grid, st );
+        case 5: return launch_structN_b<5> ( a, ed, wide, grid, st );
         default: return false;
     }
-#undef MTX_SN
+}
+
+// 64-bit planes of the factor of length l ending at every position (zero
+// where it would start before position 0); top-aligned for Hamming.
+__global__ void k_wplanes_all64 ( const uint8_t * __restrict__ codes, uint32_t total, uint32_t l, uint32_t B,
+                                  int top_aligned, unsigned long long * __restrict__ out )
+{
+    const uint32_t pos = blockIdx.x * blockDim.x + threadIdx.x;
+    if ( pos >= total ) return;
+    unsigned long long pl[kMaxPlanes] = { 0, 0, 0, 0, 0 };
+    if ( pos + 1 >= l )
+        for ( uint32_t q = 0; q < l; ++q )
+        {
+            const unsigned long long c = codes[pos + 1 - l + q];
+            const uint32_t bit = top_aligned ? ( 64 - l + q ) : q;
+#pragma unroll
+            for ( int b = 0; b < kMaxPlanes; ++b ) pl[b] |= ( ( c >> b ) & 1ull ) << bit;
+        }
+    for ( uint32_t b = 0; b < B; ++b ) out[( size_t ) b * total + pos] = pl[b];
 }
 
 // Start offset of the sequence holding each position.

@@ -124,12 +124,16 @@ struct StructFinalizeArgs
 bool launch_dp_struct1 ( const StructArgs & a, int B, bool ed, dim3 grid, cudaStream_t st );
 
 // Structured motifs with any number of gaps (dp_struct.cu, k_dp_structN).
-constexpr uint32_t kMaxStructsN = 32;
-constexpr uint32_t kMaxGapsN = 8;
+constexpr uint32_t kMaxStructsN = 128;           // structures of the any-gap kernel (shared-memory counters)
+constexpr uint32_t kMaxGapsN = 16;
+constexpr uint32_t kStructMaxBox = 64;           // box length (and l) of structured motifs
+constexpr size_t   kStructNMaxSmem = 200 * 1024; // dynamic shared memory of the any-gap kernel
 struct StructNArgs
 {
     TextView          text;
     const uint32_t *  wpl;           // box b's planes at [(b * B + plane) * total + pos]
+    const unsigned long long * wpl64; // the same with 64-bit rows (a box longer than 32)
+    bool              wide;          // rows are wpl64
     const uint8_t *   row_ok;
     const uint32_t *  row_end;       // end offset of the position's sequence
     const uint32_t *  seq_start;     // start offset of the position's sequence
@@ -177,6 +181,9 @@ struct StructNBlk
 bool structN_blk_shape ( const StructNArgs & a, const uint32_t * h_xoff, bool ed, StructNBlk * C );
 bool launch_dp_structN_blk ( const StructNArgs & a, const StructNBlk & C, int B, bool ed, dim3 grid, cudaStream_t st );
 __global__ void k_seq_start ( const uint32_t * offs, uint32_t nseq, uint64_t total, uint32_t * out );
+__global__ void k_wplanes_all64 ( const uint8_t * codes, uint32_t total, uint32_t l, uint32_t B, int top_aligned,
+                                  unsigned long long * out );
+size_t structN_smem_bytes ( const StructNArgs & a );
 __global__ void k_wplanes_all ( const uint8_t * codes, uint32_t total, uint32_t l, uint32_t B, int top_aligned,
                                 uint32_t * out );
 __global__ void k_struct_rows ( const uint32_t * offs, uint32_t nseq, uint64_t total, uint32_t l0, uint32_t tml,

@@ -79,8 +79,9 @@ enum Slot
 constexpr size_t kPinPresent = 0;          // 256 x u32 symbol presence
 constexpr size_t kPinCmap = 1024;          // 256 B symbol -> code
 constexpr size_t kPinScalar = 2048;        // u32 unique count, u32 motif count, -, staging error flag
-constexpr size_t kPinXoff = 2560;          // structure offset table (<= 384 u32)
-constexpr size_t kPinChunks = 4096;        // chunk table
+constexpr size_t kPinXoff = 4096;          // structure offset table (<= kPinXoffWords u32)
+constexpr size_t kPinXoffWords = 4096;
+constexpr size_t kPinChunks = kPinXoff + 4 * kPinXoffWords;        // chunk table
 constexpr size_t kPinStage = 65536;        // input upload / result download
 constexpr uint32_t kMaxChunks = ( kPinStage - kPinChunks ) / sizeof ( ChunkInfo );
 
@@ -303,20 +304,21 @@ int validate ( const motex_params * p )
         if ( ! p->gap_min || ! p->gap_max || ! p->blens || ! p->berrs ) return fail ( MOTEX_EINVAL, "null box arrays" );
         if ( p->nb_gaps > kMaxGapsN )
             return fail ( MOTEX_EUNSUPPORTED, "structured motifs with %u gaps (at most %u)", p->nb_gaps, kMaxGapsN );
-        if ( p->l > 32 ) return fail ( MOTEX_EUNSUPPORTED, "structured motifs need l <= 32" );
+        if ( p->l > kStructMaxBox ) return fail ( MOTEX_EUNSUPPORTED, "structured motifs need l <= %u", kStructMaxBox );
         uint64_t structs = 1, tml = p->l;
         for ( uint32_t g = 0; g < p->nb_gaps; ++g )
         {
             if ( p->gap_max[g] < p->gap_min[g] ) return fail ( MOTEX_EINVAL, "gap range [%u,%u] is empty", p->gap_min[g], p->gap_max[g] );
             if ( p->blens[g] == 0 ) return fail ( MOTEX_EINVAL, "box length must be positive" );
-            if ( p->blens[g] > 32 ) return fail ( MOTEX_EUNSUPPORTED, "structured boxes need box length <= 32" );
+            if ( p->blens[g] > kStructMaxBox )
+                return fail ( MOTEX_EUNSUPPORTED, "structured boxes need box length <= %u", kStructMaxBox );
             structs *= p->gap_max[g] - p->gap_min[g] + 1;
             if ( structs > 1u << 20 ) break;
             tml += p->gap_min[g] + p->blens[g];
         }
-        if ( ! struct1_shape ( p ) && structs > kMaxStructsN )
-            return fail ( MOTEX_EUNSUPPORTED, "%llu gap structures (at most %u with several gaps or long gaps)",
-                          ( unsigned long long ) structs, kMaxStructsN );
+        if ( ! struct1_shape ( p ) && ( structs > kMaxStructsN || structs * p->nb_gaps > kPinXoffWords ) )
+            return fail ( MOTEX_EUNSUPPORTED, "%llu gap structures (at most %u with several gaps, long gaps or boxes "
+                          "longer than 32)", ( unsigned long long ) structs, kMaxStructsN );
         for ( uint32_t g = 0; g < p->nb_gaps; ++g )
             if ( p->berrs[g] >= tml )
                 return fail ( MOTEX_EUNSUPPORTED, "box error bound %u not below the minimum motif length", p->berrs[g] );
@@ -944,14 +946,24 @@ int plan_structured_n ( Job * j )
     const uint8_t * codes = dptr<uint8_t> ( j, S_CODES );
     uint32_t *wpl, *row_end, *seq_start, *xoff;
     uint8_t * row_ok;
-    MTX_TRY ( ensure ( j, S_WPLN, ( size_t ) ( NG + 1 ) * B * T, &wpl ) );
+    // rows of 64 bits when a box (or l) is longer than 32 symbols
+    uint32_t maxlen = P.l;
+    for ( uint32_t g = 0; g < NG; ++g ) maxlen = std::max ( maxlen, j->blens[g] );
+    const bool wide = maxlen > 32;
+    MTX_TRY ( ensure ( j, S_WPLN, ( size_t ) ( NG + 1 ) * B * T * ( wide ? 2 : 1 ), &wpl ) );
     MTX_TRY ( ensure ( j, S_ROWOK, T, &row_ok ) );
     MTX_TRY ( ensure ( j, S_ROWEND, T, &row_end ) );
     MTX_TRY ( ensure ( j, S_SEQSTART, T, &seq_start ) );
     MTX_TRY ( ensure ( j, S_XOFF, ( size_t ) NS * NG, &xoff ) );
     for ( uint32_t b = 0; b <= NG; ++b )
-        MTX_LAUNCH ( k_wplanes_all, blocks_for ( T, 256 ), 256, codes, T, b ? j->blens[b - 1] : P.l, ( uint32_t ) B,
-                     ed ? 0 : 1, wpl + ( size_t ) b * B * T );
+    {
+        if ( wide )
+            MTX_LAUNCH ( k_wplanes_all64, blocks_for ( T, 256 ), 256, codes, T, b ? j->blens[b - 1] : P.l, ( uint32_t ) B,
+                         ed ? 0 : 1, reinterpret_cast<unsigned long long *> ( wpl ) + ( size_t ) b * B * T );
+        else
+            MTX_LAUNCH ( k_wplanes_all, blocks_for ( T, 256 ), 256, codes, T, b ? j->blens[b - 1] : P.l, ( uint32_t ) B,
+                         ed ? 0 : 1, wpl + ( size_t ) b * B * T );
+    }
     MTX_LAUNCH ( k_struct_rows, blocks_for ( T, 256 ), 256, dptr<uint32_t> ( j, S_OFFS ), j->nseq, j->total, P.l,
                  j->tml, j->npat, row_ok, row_end );
     MTX_LAUNCH ( k_seq_start, blocks_for ( T, 256 ), 256, dptr<uint32_t> ( j, S_OFFS ), j->nseq, j->total, seq_start );
@@ -987,6 +999,9 @@ int plan_structured_n ( Job * j )
     }
     sa.ngaps = NG;
     sa.nstructs = NS;
+    sa.wide = wide;
+    if ( structN_smem_bytes ( sa ) > kStructNMaxSmem )
+        return fail ( MOTEX_EUNSUPPORTED, "%u gap structures need more shared memory than a CTA has", NS );
     // block form where the shape allows: a warp owns Pw pattern positions
     j->structN_blk = structN_blk_shape ( sa, h_xoff, ed, &j->snb );
     const uint32_t per_cta = j->structN_blk ? ( kDPThreads / 32 ) * j->snb.Pw : kDPThreads;
@@ -1022,7 +1037,8 @@ int plan_structured_n ( Job * j )
     sa.text.vmask = dptr<uint32_t> ( j, S_VMASK );
     sa.text.emask = dptr<uint32_t> ( j, S_EMASK );
     sa.text.nblk = j->nblk;
-    sa.wpl = wpl;
+    sa.wpl = wide ? nullptr : wpl;
+    sa.wpl64 = wide ? reinterpret_cast<const unsigned long long *> ( wpl ) : nullptr;
     sa.row_ok = row_ok;
     sa.row_end = row_end;
     sa.seq_start = seq_start;

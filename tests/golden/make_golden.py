@@ -141,6 +141,24 @@ def planted_long_gap(seed, nseq, length, d):
                       boxes=((20, 30, 8, 1),))
 
 
+def planted_boxes(seed, nseq, length, d, k, e, boxes, q=30, frac=0.6):
+    """Random DNA with a planted structured motif of the given boxes (a
+    k-mer, then per gap a random gap of gmin..gmax symbols and a box of
+    blen symbols; <= 1 substitution per box) in `frac` of the sequences."""
+    rng = np.random.default_rng(seed)
+    seqs = [W._rand_seq(rng, W.DNA, length) for _ in range(nseq)]
+    parts = [W._rand_seq(rng, W.DNA, k)] + [W._rand_seq(rng, W.DNA, b[2]) for b in boxes]
+
+    def copy():
+        occ = W._substitute(rng, parts[0], W.DNA, int(rng.integers(2)))
+        for (gmin, gmax, _, _), box in zip(boxes, parts[1:]):
+            occ += W._rand_seq(rng, W.DNA, int(rng.integers(gmin, gmax + 1)))
+            occ += W._substitute(rng, box, W.DNA, int(rng.integers(2)))
+        return occ
+    W._plant(rng, seqs, copy, frac)
+    return W.Workload("planted_boxes", "DNA", seqs, d=d, k=k, e=e, q=q, boxes=tuple(boxes))
+
+
 def quorum_boundary(seed):
     """100 sequences; one 10-mer planted exactly in 29 of them and run with
     q=29: (29/100)*100 evaluates below 29 in IEEE double, so the reference
@@ -248,6 +266,17 @@ def cases():
     w = W.prot_uneven(seed=25, scale=0.004, d=1)
     w.k, w.e, w.q = 4, 2, 30
     out.append(("short_factor_k4_e2_prot_ed", w, [], None))
+    # structured shapes beyond 32-symbol rows, 32 structures and 8 gaps
+    box40 = ((2, 5, 40, 4), (1, 4, 6, 1), (3, 6, 7, 1))               # 3 gaps, 64 structures, a 40-symbol box
+    out.append(("struct3_box40_hd", planted_boxes(26, 10, 260, 0, 8, 1, box40), [], None))
+    out.append(("struct3_box40_ed", planted_boxes(26, 10, 260, 1, 8, 1, box40), [], None))
+    out.append(("struct_l40_hd", planted_boxes(27, 10, 220, 0, 40, 4, ((3, 6, 10, 1),)), [], None))
+    out.append(("struct_l40_ed", planted_boxes(27, 10, 220, 1, 40, 4, ((3, 6, 10, 1),)), [], None))
+    gaps9 = tuple([(1, 1, 4, 0)] * 7 + [(1, 2, 4, 0), (2, 3, 5, 1)])  # 9 gaps, 4 structures
+    out.append(("struct9_gaps_hd", planted_boxes(28, 10, 200, 0, 5, 0, gaps9), [], None))
+    out.append(("struct9_gaps_ed", planted_boxes(28, 10, 200, 1, 5, 0, gaps9), [], None))
+    many = ((0, 7, 6, 1), (0, 7, 6, 1))                                # 2 gaps, 64 structures
+    out.append(("struct2_64structs_ed", planted_boxes(29, 10, 220, 1, 6, 1, many), [], None))
     return out
 
 

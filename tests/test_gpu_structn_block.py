@@ -96,3 +96,52 @@ def test_block_equals_per_position_form(native_built, monkeypatch, d):
     assert blk[0] == per[0] == 0, blk[2] + per[2]
     assert blk[1] == per[1]
     assert blk[1].count("\n") > 20                 # motifs printed
+
+
+def wide_case(rng):
+    """Shapes only the per-position any-gap kernel takes: a box or box 0
+    longer than 32 symbols (64-bit rows), more than 32 structures, or more
+    than 8 gaps."""
+    shape = rng.choice(["wide_box", "wide_l", "many", "gaps"])
+    d = rng.randint(0, 1)
+    l, e = rng.randint(5, 8), rng.randint(0, 1)
+    if shape == "wide_l":
+        l, e = rng.randint(33, 60), rng.randint(2, 6)
+    if shape == "wide_box":
+        boxes = [(rng.randint(0, 4), 0, rng.randint(33, 64), rng.randint(1, 5))]
+        boxes = [(a, a + rng.randint(0, 3), c, dd) for a, _, c, dd in boxes]
+        if rng.random() < 0.5:
+            boxes.append((1, 3, rng.randint(4, 8), 1))
+    elif shape == "wide_l":
+        boxes = [(2, 5, rng.randint(6, 12), 1)]
+    elif shape == "many":
+        boxes = [(0, rng.randint(5, 9), rng.randint(4, 7), 1), (0, rng.randint(5, 9), rng.randint(4, 7), 1)]
+    else:
+        boxes = [(1, rng.choice([1, 1, 2]), rng.randint(3, 5), 0) for _ in range(rng.randint(9, 12))]
+    nseq = rng.randint(4, 8)
+    seqs = ["".join(rng.choice("ACGT") for _ in range(rng.randint(80, 300))) for _ in range(nseq)]
+    parts = ["".join(rng.choice("ACGT") for _ in range(l))] + ["".join(rng.choice("ACGT") for _ in range(b[2]))
+                                                               for b in boxes]
+    for i in range(nseq):
+        if rng.random() < 0.6:
+            occ = parts[0]
+            for (gmin, gmax, _, _), box in zip(boxes, parts[1:]):
+                occ += "".join(rng.choice("ACGT") for _ in range(rng.randint(gmin, gmax))) + box
+            if len(occ) <= len(seqs[i]):
+                a = rng.randint(0, len(seqs[i]) - len(occ))
+                seqs[i] = seqs[i][:a] + occ + seqs[i][a + len(occ):]
+    args = ["-a", "DNA", "-i", "in.fa", "-o", "out.motex", "-d", str(d), "-k", str(l), "-e", str(e),
+            "-q", str(rng.choice([20, 40])), "-s", "in.boxes"]
+    return seqs, boxes, args
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("seed", range(16))
+def test_wide_and_many_structures_vs_oracle(native_built, oracle_port, seed):
+    rng = random.Random(9300 + seed)
+    seqs, boxes, args = wide_case(rng)
+    files = {"in.fa": fasta(seqs), "in.boxes": boxes_text(boxes)}
+    g = run_cli(native_built.CLI_PATH, None, args, files=files)
+    o = run_cli(oracle_port, None, args + ["-t", "8"], files=files)
+    assert g[0] == o[0] == 0, g[2] + o[2]
+    assert g[1] == o[1]

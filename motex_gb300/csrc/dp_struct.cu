@@ -1238,6 +1238,79 @@ bool launch_dp_structN ( const StructNArgs & a, int B, bool ed, dim3 grid, cudaS
     }
 }
 
+namespace
+{
+
+// Symbol t of entry (pos, k)'s key: box 0 first, then each later box.
+__device__ __forceinline__ uint32_t skey_sym_pos ( const SKeyArgs & a, uint32_t pos, uint32_t k, uint32_t t )
+{
+    if ( t < a.l ) return pos + 1 - a.l + t;
+    t -= a.l;
+    for ( uint32_t g = 0; g < a.NG; ++g )
+    {
+        if ( t < a.blen[g] ) return pos + a.xoff[k * a.NG + g] + 1 - a.blen[g] + t;
+        t -= a.blen[g];
+    }
+    return pos;                                                     // not reached: t < key length
+}
+
+__device__ __forceinline__ uint32_t skey_len ( const SKeyArgs & a )
+{
+    uint32_t n = a.l;
+    for ( uint32_t g = 0; g < a.NG; ++g ) n += a.blen[g];
+    return n;
+}
+
+} // namespace
+
+// Insert every passing entry's key: the slot keeps a representative entry
+// (compared symbol by symbol on a hash match) and the least entry index.
+__global__ void k_skey_insert ( SKeyArgs a )
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if ( i >= a.nrec ) return;
+    const uint32_t idx = a.recs[3 * ( size_t ) i];
+    const uint32_t pos = idx / a.G, k = idx % a.G;
+    const uint32_t L = skey_len ( a );
+    unsigned long long h = 0xcbf29ce484222325ull;                  // FNV-1a over the key's codes
+    for ( uint32_t t = 0; t < L; ++t )
+    {
+        h ^= a.codes[skey_sym_pos ( a, pos, k, t )];
+        h *= 0x100000001b3ull;
+    }
+    const uint32_t tsize = 1u << a.tbits;
+    uint32_t slot = ( uint32_t ) ( ( h * 0x9E3779B97F4A7C15ull ) >> ( 64 - a.tbits ) );
+    for ( uint32_t probe = 0; probe < tsize; ++probe )
+    {
+        const uint32_t r = atomicCAS ( a.rep + slot, 0xffffffffu, i );
+        bool same = r == 0xffffffffu;
+        if ( ! same )
+        {
+            const uint32_t ridx = a.recs[3 * ( size_t ) r];
+            const uint32_t rpos = ridx / a.G, rk = ridx % a.G;
+            same = true;
+            for ( uint32_t t = 0; t < L && same; ++t )
+                same = a.codes[skey_sym_pos ( a, pos, k, t )] == a.codes[skey_sym_pos ( a, rpos, rk, t )];
+        }
+        if ( same )
+        {
+            atomicMin ( a.first + slot, i );
+            a.slot_of[i] = slot;
+            return;
+        }
+        slot = ( slot + 1 ) & ( tsize - 1 );
+    }
+    atomicExch ( a.err, 1u );
+    a.slot_of[i] = 0;
+}
+
+__global__ void k_skey_keep ( SKeyArgs a )
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if ( i >= a.nrec ) return;
+    a.keep[i] = a.first[a.slot_of[i]] == i ? 1 : 0;
+}
+
 // 64-bit planes of the factor of length l ending at every position (zero
 // where it would start before position 0); top-aligned for Hamming.
 __global__ void k_wplanes_all64 ( const uint8_t * __restrict__ codes, uint32_t total, uint32_t l, uint32_t B,

@@ -184,6 +184,26 @@ __global__ void k_seq_start ( const uint32_t * offs, uint32_t nseq, uint64_t tot
 __global__ void k_wplanes_all64 ( const uint8_t * codes, uint32_t total, uint32_t l, uint32_t B, int top_aligned,
                                   unsigned long long * out );
 size_t structN_smem_bytes ( const StructNArgs & a );
+
+// Device deduplication of passing structured entries by the writer's key
+// (the boxes' symbols, gaps left out; functions.cc:1191-1239): the first
+// entry of a key in print order is kept.
+struct SKeyArgs
+{
+    const uint32_t * recs;           // 3 words per entry: pos * G + k, u, v (print order)
+    uint32_t         nrec, G, NG, l;
+    uint32_t         blen[kMaxGapsN];
+    const uint8_t *  codes;
+    const uint32_t * xoff;           // [k * NG + g]: end of box g+1 minus end of box 0
+    uint32_t         tbits;          // 2^tbits table slots
+    uint32_t *       rep;            // a representative entry of the slot's key (~0: empty)
+    uint32_t *       first;          // least entry index with the slot's key
+    uint32_t *       slot_of;        // slot of each entry
+    uint8_t *        keep;
+    uint32_t *       err;            // set to 1 if a probe ever visited every slot
+};
+__global__ void k_skey_insert ( SKeyArgs a );
+__global__ void k_skey_keep ( SKeyArgs a );
 __global__ void k_wplanes_all ( const uint8_t * codes, uint32_t total, uint32_t l, uint32_t B, int top_aligned,
                                 uint32_t * out );
 __global__ void k_struct_rows ( const uint32_t * offs, uint32_t nseq, uint64_t total, uint32_t l0, uint32_t tml,

@@ -26,7 +26,6 @@
 #include <mutex>
 #include <string>
 #include <tuple>
-#include <unordered_set>
 #include <vector>
 
 using namespace mtx;
@@ -72,13 +71,14 @@ enum Slot
     S_RAW, S_OFFS, S_WSTART, S_QOK, S_CMAP, S_PRESENT, S_CODES, S_PLANES, S_VMASK, S_EMASK,
     S_WPOS, S_KEY0, S_KEY1, S_IDX1, S_HIST, S_HEAD, S_PREF, S_UNIQ, S_WPL32, S_WPL64,
     S_CHUNKS, S_UACC, S_VACC, S_FLAGS, S_MARK, S_RECU, S_RECV, S_PREF2, S_RECS, S_TILES,
-    S_SCALAR, S_UOUT, S_VOUT, S_WPL0, S_WPL1, S_ROWOK, S_ROWEND, S_WPLN, S_SEQSTART, S_XOFF, S_HTILES, S_COUNT
+    S_SCALAR, S_UOUT, S_VOUT, S_WPL0, S_WPL1, S_ROWOK, S_ROWEND, S_WPLN, S_SEQSTART, S_XOFF, S_HTILES,
+    S_STAB, S_SSLOT, S_SKEEP, S_COUNT
 };
 
 // Pinned staging layout of a job (bytes).
 constexpr size_t kPinPresent = 0;          // 256 x u32 symbol presence
 constexpr size_t kPinCmap = 1024;          // 256 B symbol -> code
-constexpr size_t kPinScalar = 2048;        // u32 unique count, u32 motif count, -, staging error flag
+constexpr size_t kPinScalar = 2048;        // u32 unique count, u32 motif count, key-table error flag, staging error flag
 constexpr size_t kPinXoff = 4096;          // structure offset table (<= kPinXoffWords u32)
 constexpr size_t kPinXoffWords = 4096;
 constexpr size_t kPinChunks = kPinXoff + 4 * kPinXoffWords;        // chunk table
@@ -114,7 +114,6 @@ struct Job
     uint32_t npat = 0;                         // leading pattern sequences (0: all-pairs)
     uint64_t ref_cells = 0;
     uint32_t G = 1;                            // gap choices (1 for single motifs)
-    std::vector<char> raw_host;                // structured runs: input copy for key dedup
 
     // executed
     int B = 0;
@@ -874,6 +873,14 @@ int plan_structured ( Job * j )
     MTX_LAUNCH ( k_wplanes_all, blocks_for ( T, 256 ), 256, codes, T, b1, ( uint32_t ) B, ed ? 0 : 1, wpl1 );
     MTX_LAUNCH ( k_struct_rows, blocks_for ( T, 256 ), 256, dptr<uint32_t> ( j, S_OFFS ), j->nseq, j->total, P.l,
                  j->tml, j->npat, row_ok, row_end );
+    // end offset of box 1 for every gap choice k (the key deduplication reads it)
+    {
+        uint32_t * xoff;
+        MTX_TRY ( ensure ( j, S_XOFF, G, &xoff ) );
+        uint32_t * h_xoff = pin<uint32_t> ( j, kPinXoff );
+        for ( uint32_t k = 0; k < G; ++k ) h_xoff[k] = gmin + k + b1;
+        MTX_CUDA ( cudaMemcpyAsync ( xoff, h_xoff, ( size_t ) G * 4, cudaMemcpyHostToDevice, st ) );
+    }
 
     const uint32_t ctas_x = ( T + kDPThreads - 1 ) / kDPThreads;
     j->ntiles = ctas_x;
@@ -1172,9 +1179,8 @@ int stage_finalize ( Job * j, bool * need_sync )
 
 int stage_compact ( Job * j )
 {
-    // the packer's staging-wait flag comes back with the results
-    MTX_CUDA ( cudaMemcpyAsync ( pin<uint32_t> ( j, kPinScalar ) + 3, dptr<uint32_t> ( j, S_SCALAR ) + 3, 4,
-                                 cudaMemcpyDeviceToHost, j->ctx->st ) );
+    uint32_t * scalar = dptr<uint32_t> ( j, S_SCALAR );
+    MTX_CUDA ( cudaMemsetAsync ( scalar + 2, 0, 4, j->ctx->st ) );
     if ( ! j->npat )
     {
         if ( ! j->replaying ) j->nrec = pin<uint32_t> ( j, kPinScalar )[1];
@@ -1183,7 +1189,36 @@ int stage_compact ( Job * j )
         MTX_TRY ( ensure ( j, S_RECS, ( size_t ) 3 * std::max<uint32_t> ( 1, j->nrec ), &recs ) );
         MTX_LAUNCH ( k_compact, blocks_for ( n, 256 ), 256, dptr<uint8_t> ( j, S_MARK ), dptr<uint32_t> ( j, S_PREF2 ), n,
                      dptr<uint32_t> ( j, S_RECU ), dptr<uint32_t> ( j, S_RECV ), recs );
+        if ( j->structured && j->nrec )
+        {
+            // the writer's key deduplication (functions.cc:1191-1239) on the
+            // device: a hash table of the entries' box symbols keeps the
+            // first entry of every key in print order
+            SKeyArgs ka {};
+            ka.recs = recs;
+            ka.nrec = j->nrec;
+            ka.G = j->G;
+            ka.NG = j->prm.nb_gaps;
+            ka.l = j->prm.l;
+            for ( uint32_t g = 0; g < ka.NG; ++g ) ka.blen[g] = j->blens[g];
+            ka.codes = dptr<uint8_t> ( j, S_CODES );
+            ka.xoff = dptr<uint32_t> ( j, S_XOFF );
+            ka.tbits = 5;
+            while ( ( 1ull << ka.tbits ) < 2ull * j->nrec ) ++ka.tbits;
+            uint32_t * tab;
+            MTX_TRY ( ensure ( j, S_STAB, ( size_t ) 2 << ka.tbits, &tab ) );
+            MTX_TRY ( ensure ( j, S_SSLOT, j->nrec, &ka.slot_of ) );
+            MTX_TRY ( ensure ( j, S_SKEEP, j->nrec, &ka.keep ) );
+            ka.rep = tab;
+            ka.first = tab + ( ( size_t ) 1 << ka.tbits );
+            ka.err = scalar + 2;
+            MTX_CUDA ( cudaMemsetAsync ( tab, 0xff, ( size_t ) 8 << ka.tbits, j->ctx->st ) );
+            MTX_LAUNCH ( k_skey_insert, blocks_for ( j->nrec, 256 ), 256, ka );
+            MTX_LAUNCH ( k_skey_keep, blocks_for ( j->nrec, 256 ), 256, ka );
+        }
     }
+    // the key-table and packer staging-wait flags come back with the results
+    MTX_CUDA ( cudaMemcpyAsync ( pin<uint32_t> ( j, kPinScalar ) + 2, scalar + 2, 8, cudaMemcpyDeviceToHost, j->ctx->st ) );
     MTX_TRY ( record ( j, j->ev1 ) );
     return MOTEX_OK;
 }
@@ -1194,6 +1229,7 @@ int read_times ( Job * j )
     if ( const uint32_t e = pin<uint32_t> ( j, kPinScalar )[3] )
         return fail ( MOTEX_ETIMEOUT, "packing: a TMA staging wait gave up (copy not completed)%s",
                       ( e & 2u ) ? "; so did the drain of the copies in flight" : "" );
+    if ( pin<uint32_t> ( j, kPinScalar )[2] ) return fail ( MOTEX_ECUDA, "structured key table overflow" );
     MTX_CUDA ( cudaEventElapsedTime ( &j->device_ms, j->ev0, j->ev1 ) );
     if ( j->dp_timed ) MTX_CUDA ( cudaEventElapsedTime ( &j->dp_ms, j->evd0, j->evd1 ) );
     return MOTEX_OK;
@@ -1352,8 +1388,6 @@ int load_job ( Job * j, const motex_params * prm, const char * const * seqs, con
         memcpy ( stage + at, seqs[i], lens[i] );
         at += lens[i];
     }
-    if ( prm->nb_gaps && ! npat ) j->raw_host.assign ( stage, stage + total );
-    else j->raw_host.clear ();
     memcpy ( stage + raw_b, j->offs.data (), ( size_t ) ( nseq + 1 ) * 4 );
     memcpy ( stage + raw_b + offs_b, wstart.data (), ( size_t ) ( nseq + 1 ) * 4 );
     memcpy ( stage + raw_b + 2 * offs_b, qok.data (), nseq + 1 );
@@ -1378,9 +1412,13 @@ int fetch_issue ( Job * j )
 {
     if ( j->nrec == 0 ) return MOTEX_OK;
     const size_t bytes = ( size_t ) j->nrec * 12;
-    MTX_TRY ( ensure_pinned ( j, kPinStage + bytes ) );
+    const bool keyed = j->prm.nb_gaps && ! j->npat;              // structured: the device's keep flags too
+    MTX_TRY ( ensure_pinned ( j, kPinStage + bytes + ( keyed ? j->nrec : 0 ) ) );
     MTX_CUDA ( cudaMemcpyAsync ( pin<uint32_t> ( j, kPinStage ), dptr<uint32_t> ( j, S_RECS ), bytes,
                                  cudaMemcpyDeviceToHost, j->ctx->st ) );
+    if ( keyed )
+        MTX_CUDA ( cudaMemcpyAsync ( pin<uint8_t> ( j, kPinStage + bytes ), dptr<uint8_t> ( j, S_SKEEP ), j->nrec,
+                                     cudaMemcpyDeviceToHost, j->ctx->st ) );
     return MOTEX_OK;
 }
 
@@ -1413,37 +1451,15 @@ int fetch_build ( Job * j, motex_result * out )
     out->motifs = static_cast<motex_motif *> ( malloc ( ( size_t ) j->nrec * sizeof ( motex_motif ) ) );
     if ( ! out->motifs ) return fail ( MOTEX_ENOMEM, "host allocation of the result failed" );
     const uint32_t G = j->prm.nb_gaps ? j->G : 1;
-    std::unordered_set<std::string> seen;
-    std::string key;
+    // structured: the first entry of every key in print order, flagged on the device
+    const uint8_t * keep = j->prm.nb_gaps && ! j->npat ? pin<uint8_t> ( j, kPinStage + ( size_t ) j->nrec * 12 ) : nullptr;
     uint32_t s = 0, kept = 0;
     for ( uint32_t i = 0; i < j->nrec; ++i )
     {
         const uint32_t idx = h[3 * i];
         const uint32_t pos = idx / G, k = idx % G;
         while ( j->offs[s + 1] <= pos ) ++s;        // records are in (position, gap choice) order
-        if ( j->prm.nb_gaps )
-        {
-            // the writer's key: the boxes joined by '_', gaps left out
-            // (functions.cc:1191-1239); the first passing entry of a key wins
-            const uint32_t l = j->prm.l, NG = j->prm.nb_gaps;
-            const char * x = j->raw_host.data ();
-            key.assign ( x + pos + 1 - l, l );
-            uint32_t rem = k, end = pos;
-            uint32_t S[kMaxGapsN];
-            for ( int g = ( int ) NG - 1; g >= 0; --g )
-            {
-                const uint32_t span = j->gmax[g] - j->gmin[g] + 1;
-                S[g] = j->gmin[g] + rem % span;
-                rem /= span;
-            }
-            for ( uint32_t g = 0; g < NG; ++g )
-            {
-                key.push_back ( '_' );
-                key.append ( x + end + 1 + S[g], j->blens[g] );
-                end += S[g] + j->blens[g];
-            }
-            if ( ! seen.insert ( key ).second ) continue;
-        }
+        if ( keep && ! keep[i] ) continue;
         out->motifs[kept++] = motex_motif { s, pos - j->offs[s], k, h[3 * i + 1], h[3 * i + 2] };
     }
     out->count = kept;
@@ -1713,7 +1729,8 @@ int run_mini ( motex_ctx * c, std::vector<Job *> & js, float * dp_ms )
         m.ctas = ( uint32_t ) std::min<uint64_t> ( kMiniMaxCtas, std::max<uint64_t> ( 1, ( j->total + 4095 ) / 4096 ) );
         max_ctas = std::max ( max_ctas, m.ctas );
         memcpy ( m.cmap, pin<uint8_t> ( j, kPinCmap ), 256 );
-        pin<uint32_t> ( j, kPinScalar )[3] = 0;                     // no staging wait in this pipeline
+        pin<uint32_t> ( j, kPinScalar )[2] = 0;                     // no key table and no staging wait
+        pin<uint32_t> ( j, kPinScalar )[3] = 0;                     // in this pipeline
     }
     MTX_CUDA ( cudaMemcpyAsync ( dd, hd, ( size_t ) n * sizeof ( MiniJob ), cudaMemcpyHostToDevice, st ) );
     MTX_CUDA ( cudaMemsetAsync ( dres, 0, resb, st ) );

@@ -204,6 +204,25 @@ __device__ __forceinline__ void bulk_copy_g2s ( void * dst, const void * src, ui
                    : "memory" );
 }
 
+// Key of the factor ending at each lane's position (its last `win`
+// symbols, B bits each, the last one lowest): c = this step's codes, pk =
+// the previous step's keys.  Window sizes double per level; a lane below s
+// takes the low s symbols of the previous step's key.
+__device__ __forceinline__ unsigned long long pack_keys ( uint32_t c, unsigned long long pk, uint32_t win, uint32_t B,
+                                                          unsigned long long keymask, int lane )
+{
+    unsigned long long y = c;
+    for ( uint32_t s = 1; s < win; s <<= 1 )
+    {
+        const unsigned long long cur = __shfl_up_sync ( 0xffffffffu, y, s );
+        const unsigned long long old = __shfl_sync ( 0xffffffffu, pk, ( lane + 32 - ( int ) s ) & 31 );
+        const unsigned long long low = ( 1ull << ( s * B ) ) - 1ull;
+        const unsigned long long src = lane >= ( int ) s ? cur : ( old & low );
+        y = ( y | ( src << ( s * B ) ) ) & keymask;
+    }
+    return y & keymask;
+}
+
 } // namespace
 
 /*
@@ -215,7 +234,10 @@ __device__ __forceinline__ void bulk_copy_g2s ( void * dst, const void * src, ui
  * 32-byte row per step), writes its code and its factor-end entry (both
  * coalesced), and the warp forms block k0+i's bit planes, validity and end
  * masks by ballot; lane i keeps them, so every plane and mask row leaves as
- * one coalesced 128-byte store per warp.
+ * one coalesced 128-byte store per warp.  With a.key0 set the warp also
+ * forms the first radix-sort key of every factor from the codes of its lanes
+ * (a shift-or doubling over the warp, the previous step's keys for the
+ * lanes below the window), so the sort starts without a gather pass.
  *
  * Failure path: a staging wait that gives up (a.wait_polls polls) sets bit 0
  * of *a.err.  The CTA then issues no further copy and packs the rest of its
@@ -296,6 +318,16 @@ __global__ void __launch_bounds__ ( kPackThreads ) k_pack ( PackArgs a )
         uint64_t start = a.offs[s], end = a.offs[s + 1];
         uint32_t ws = a.wstart[s];
         uint32_t pl[kMaxPlanes] = {}, vm_mine = 0, em_mine = 0;
+        // keys of the block before the warp's first one (its lanes' low
+        // windows, the part the doubling reads, need no earlier block)
+        const bool want_keys = a.key0 != nullptr;
+        const unsigned long long keymask = ( 1ull << ( a.kwin * ( uint32_t ) a.B ) ) - 1ull;
+        unsigned long long pk = 0;
+        if ( want_keys && k0 > 0 )
+        {
+            const uint64_t pp = ( k0 - 1 ) * 32 + lane;
+            pk = pack_keys ( pp < a.total ? cmap[a.raw[pp]] : 0u, 0ull, a.kwin, a.B, keymask, lane );
+        }
 #pragma unroll 4
         for ( int i = 0; i < 32; ++i, pos += 32 )
         {
@@ -312,6 +344,15 @@ __global__ void __launch_bounds__ ( kPackThreads ) k_pack ( PackArgs a )
                 }
                 code = cmap[row[i * 32 + lane]];
                 a.codes[pos] = ( uint8_t ) code;
+            }
+            unsigned long long key = 0;
+            if ( want_keys )
+            {
+                key = pack_keys ( code, pk, a.kwin, a.B, keymask, lane );
+                pk = key;
+            }
+            if ( pos < a.total )
+            {
                 const uint64_t rel = pos - start;
                 const bool is_short = ( end - start ) < a.tml;
                 // pattern mode: sequences below npat are patterns (factors
@@ -319,7 +360,10 @@ __global__ void __launch_bounds__ ( kPackThreads ) k_pack ( PackArgs a )
                 valid = ! is_short && rel >= a.vstart && s >= a.npat;
                 is_end = pos == end - 1;
                 if ( ! is_short && rel + 1 >= a.l && ( a.npat == 0 || s < a.npat ) )
+                {
                     a.wpos[ws + ( uint32_t ) ( rel + 1 - a.l )] = ( uint32_t ) pos;
+                    if ( want_keys ) a.key0[ws + ( uint32_t ) ( rel + 1 - a.l )] = ( uint32_t ) key;
+                }
             }
 #pragma unroll
             for ( int b = 0; b < kMaxPlanes; ++b )
@@ -378,22 +422,18 @@ __global__ void k_gather_key ( const uint32_t * __restrict__ idx, uint32_t n, co
 }
 
 // Per-tile digit histogram, digit-major: hist[d * ntiles + tile].  Keys are
-// read as 16-byte vectors where the tile allows; equal digits within a warp
-// are counted by one shared atomic of their leader (repetitive inputs put
-// most keys of a warp on a few digits).
+// read as 16-byte vectors where the tile allows; each warp counts into its
+// own copy of the 256 bins (shared atomics), summed at the end.
 __global__ void __launch_bounds__ ( kSortThreads ) k_radix_hist ( const uint32_t * __restrict__ keys, uint32_t n,
                                                                    int shift, uint32_t * hist, uint32_t ntiles )
 {
-    __shared__ uint32_t cnt[256];
-    for ( int d = threadIdx.x; d < 256; d += kSortThreads ) cnt[d] = 0;
+    constexpr int NW = kSortThreads / 32;
+    __shared__ uint32_t cnt[NW][256];
+    const int warp = threadIdx.x >> 5;
+    for ( int d = threadIdx.x; d < NW * 256; d += kSortThreads ) ( &cnt[0][0] )[d] = 0;
     __syncthreads ();
     const uint32_t base = blockIdx.x * kSortTile;
-    const uint32_t lt = lanemask_lt ();
-    auto add = [&] ( bool valid, uint32_t k ) {
-        const uint32_t d = valid ? ( ( k >> shift ) & 255u ) : 256u;
-        const uint32_t peers = __match_any_sync ( 0xffffffffu, d );
-        if ( valid && ( peers & lt ) == 0 ) atomicAdd ( &cnt[d], __popc ( peers ) );
-    };
+    uint32_t * mine = cnt[warp];
     if ( base + kSortTile <= n )
     {
         const uint4 * k4 = reinterpret_cast<const uint4 *> ( keys + base );
@@ -401,10 +441,10 @@ __global__ void __launch_bounds__ ( kSortThreads ) k_radix_hist ( const uint32_t
         for ( int r = 0; r < kSortItems / 4; ++r )
         {
             const uint4 q = __ldg ( k4 + r * kSortThreads + threadIdx.x );
-            add ( true, q.x );
-            add ( true, q.y );
-            add ( true, q.z );
-            add ( true, q.w );
+            atomicAdd ( &mine[( q.x >> shift ) & 255u], 1u );
+            atomicAdd ( &mine[( q.y >> shift ) & 255u], 1u );
+            atomicAdd ( &mine[( q.z >> shift ) & 255u], 1u );
+            atomicAdd ( &mine[( q.w >> shift ) & 255u], 1u );
         }
     }
     else
@@ -412,24 +452,31 @@ __global__ void __launch_bounds__ ( kSortThreads ) k_radix_hist ( const uint32_t
         for ( int r = 0; r < kSortItems; ++r )
         {
             const uint32_t i = base + r * kSortThreads + threadIdx.x;
-            add ( i < n, i < n ? keys[i] : 0u );
+            if ( i < n ) atomicAdd ( &mine[( keys[i] >> shift ) & 255u], 1u );
         }
     }
     __syncthreads ();
-    for ( int d = threadIdx.x; d < 256; d += kSortThreads ) hist[( size_t ) d * ntiles + blockIdx.x] = cnt[d];
+    for ( int d = threadIdx.x; d < 256; d += kSortThreads )
+    {
+        uint32_t t = 0;
+#pragma unroll
+        for ( int w = 0; w < NW; ++w ) t += cnt[w][d];
+        hist[( size_t ) d * ntiles + blockIdx.x] = t;
+    }
 }
 
 /*
- * Stable scatter of one 8-bit digit.  The CTA first sorts its tile by the
- * digit in shared memory: items are ranked in input order (round r, then
- * thread index; ranks among equal digits from warp match masks plus per-warp
- * counts) and stored at their digit's tile-local offset.  Then consecutive
- * threads write consecutive items of the locally sorted tile, so every
- * digit's run of the tile leaves as contiguous stores instead of scattered
- * 4-byte writes.  The tile's digit counts and global bases come from the
- * digit-major scanned histogram: offsets[d * ntiles + t] is the first output
- * slot of digit d from tile t, and the next entry of the flattened array
- * (or n after the last) ends it.
+ * Stable scatter of one 8-bit digit.  The CTA sorts its tile by the digit in
+ * shared memory, then writes every digit's run of the tile as contiguous
+ * stores.  Warp w owns the tile's items w*512 .. w*512+511 (16 rounds of 32,
+ * kept in registers): in pass 1 each item gets its rank among the warp's
+ * items of its digit so far (warp match masks and a per-warp running count
+ * per digit); the per-warp counts then give each warp's offset within each
+ * digit and the digits' tile-local starts (three CTA barriers per tile in
+ * all); pass 2 stores every item at start[d] + warp offset + its rank.  The
+ * tile's global base per digit comes from the digit-major scanned
+ * histogram: offsets[d * ntiles + t] is the first output slot of digit d
+ * from tile t.
  */
 __global__ void __launch_bounds__ ( kSortThreads ) k_radix_scatter ( const uint32_t * __restrict__ keys_in,
                                                                       const uint32_t * __restrict__ vals_in,
@@ -440,85 +487,93 @@ __global__ void __launch_bounds__ ( kSortThreads ) k_radix_scatter ( const uint3
                                                                       uint32_t ntiles )
 {
     constexpr int NW = kSortThreads / 32;
+    constexpr int PER_WARP = kSortTile / NW;                     // 512 items, 16 rounds of 32
+    constexpr int ROUNDS = PER_WARP / 32;
     __shared__ uint32_t s_base[256];                 // global first slot of digit d from this tile
     __shared__ uint32_t s_start[256];                // tile-local first slot of digit d
-    __shared__ uint32_t s_run[256];
-    __shared__ uint32_t s_wcnt[NW][256];
+    __shared__ uint32_t s_wh[NW][256];               // per warp: running count, then offset, of digit d
     __shared__ uint32_t s_wtot[NW];
     __shared__ uint32_t s_key[kSortTile];
     __shared__ uint32_t s_val[kSortTile];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t full = 0xffffffffu;
     const uint32_t tile = blockIdx.x;
     const uint32_t base = tile * kSortTile;
     const uint32_t tn = min ( ( uint32_t ) kSortTile, n - base );
-    const uint32_t nhist = 256u * ntiles;
-    // tile-local digit counts from the scanned histogram, then their exclusive
-    // scan over the 256 digits (one digit per thread, warp scans + warp totals)
+    for ( int i = threadIdx.x; i < NW * 256; i += kSortThreads ) ( &s_wh[0][0] )[i] = 0;
     {
         const uint32_t d = threadIdx.x;                          // kSortThreads == 256
-        const size_t f = ( size_t ) d * ntiles + tile;
-        const uint32_t b = offsets[f];
-        const uint32_t c = ( f + 1 < nhist ? offsets[f + 1] : n ) - b;
-        s_base[d] = b;
-        s_run[d] = 0;
+        s_base[d] = offsets[( size_t ) d * ntiles + tile];
+    }
+    __syncthreads ();
+    // pass 1: ranks within the warp's items of each digit, in input order
+    const uint32_t lt = lanemask_lt ();
+    uint32_t key[ROUNDS], val[ROUNDS], loc[ROUNDS];
+    uint32_t * wh = s_wh[warp];
 #pragma unroll
-        for ( int w = 0; w < NW; ++w ) s_wcnt[w][d] = 0;
+    for ( int r = 0; r < ROUNDS; ++r )
+    {
+        const uint32_t li = warp * PER_WARP + r * 32 + lane;
+        const bool valid = li < tn;
+        key[r] = valid ? keys_in[base + li] : 0u;
+        val[r] = valid ? vals_in[base + li] : 0u;
+        const uint32_t d = valid ? ( ( key[r] >> shift ) & 255u ) : ( 256u + lane );
+        const uint32_t peers = __match_any_sync ( full, d );
+        const uint32_t before = valid ? wh[d] : 0u;
+        __syncwarp ();
+        if ( valid && ( peers & lt ) == 0 ) wh[d] = before + __popc ( peers );
+        __syncwarp ();
+        loc[r] = before + __popc ( peers & lt );
+    }
+    __syncthreads ();
+    // per digit: warp offsets (exclusive over warps) and the tile count, then
+    // the digits' exclusive scan (one digit per thread: warp scans + totals)
+    {
+        const uint32_t d = threadIdx.x;
+        uint32_t run = 0;
+#pragma unroll
+        for ( int w = 0; w < NW; ++w )
+        {
+            const uint32_t t = s_wh[w][d];
+            s_wh[w][d] = run;
+            run += t;
+        }
+        const uint32_t c = run;
         uint32_t x = c;
 #pragma unroll
         for ( int o = 1; o < 32; o <<= 1 )
         {
-            const uint32_t y = __shfl_up_sync ( 0xffffffffu, x, o );
+            const uint32_t y = __shfl_up_sync ( full, x, o );
             if ( lane >= o ) x += y;
         }
-        if ( lane == 31 ) s_wtot[warp] = x;                      // warp total
+        if ( lane == 31 ) s_wtot[warp] = x;
         __syncthreads ();
         uint32_t add = 0;
         for ( int w = 0; w < warp; ++w ) add += s_wtot[w];
-        s_start[d] = add + x - c;                                // exclusive over all digits
+        s_start[d] = add + x - c;
     }
     __syncthreads ();
-    const uint32_t lt = lanemask_lt ();
-    for ( int r = 0; r < kSortItems; ++r )
-    {
-        const uint32_t li = r * kSortThreads + threadIdx.x;
-        const bool valid = li < tn;
-        const uint32_t k = valid ? keys_in[base + li] : 0u;
-        const uint32_t v = valid ? vals_in[base + li] : 0u;
-        const uint32_t d = valid ? ( ( k >> shift ) & 255u ) : ( 256u + lane );
-        const uint32_t peers = __match_any_sync ( 0xffffffffu, d );
-        const uint32_t rank = __popc ( peers & lt );
-        if ( valid && rank == 0 ) s_wcnt[warp][d] = __popc ( peers );
-        __syncthreads ();
-        if ( valid )
-        {
-            uint32_t off = s_run[d];
-            for ( int w = 0; w < warp; ++w ) off += s_wcnt[w][d];
-            const uint32_t pos = s_start[d] + off + rank;
-            s_key[pos] = k;
-            s_val[pos] = v;
-        }
-        __syncthreads ();
-        for ( int dd = threadIdx.x; dd < 256; dd += kSortThreads )
-        {
-            uint32_t t = 0;
+    // pass 2: the locally sorted tile in shared memory
 #pragma unroll
-            for ( int w = 0; w < NW; ++w )
-            {
-                t += s_wcnt[w][dd];
-                s_wcnt[w][dd] = 0;
-            }
-            s_run[dd] += t;
+    for ( int r = 0; r < ROUNDS; ++r )
+    {
+        const uint32_t li = warp * PER_WARP + r * 32 + lane;
+        if ( li < tn )
+        {
+            const uint32_t d = ( key[r] >> shift ) & 255u;
+            const uint32_t pos = s_start[d] + wh[d] + loc[r];
+            s_key[pos] = key[r];
+            s_val[pos] = val[r];
         }
-        __syncthreads ();
     }
-    // the locally sorted tile: item i of digit d goes to s_base[d] + (i - s_start[d])
+    __syncthreads ();
+    // item i of digit d goes to s_base[d] + (i - s_start[d]): contiguous runs
     for ( uint32_t i = threadIdx.x; i < tn; i += kSortThreads )
     {
         const uint32_t k = s_key[i];
         const uint32_t d = ( k >> shift ) & 255u;
-        const uint32_t dst = s_base[d] + ( i - s_start[d] );
-        keys_out[dst] = k;
-        vals_out[dst] = s_val[i];
+        keys_out[s_base[d] + ( i - s_start[d] )] = k;
+        vals_out[s_base[d] + ( i - s_start[d] )] = s_val[i];
     }
 }
 

@@ -31,6 +31,8 @@ struct PackArgs
     uint32_t         nblk;
     uint32_t *       err;          // bit 0: a staging wait gave up; bit 1: its drain gave up too
     uint32_t         wait_polls;   // try_wait polls before a staging wait gives up
+    uint32_t *       key0;         // null, or the first sort key of every factor (beside wpos): its
+    uint32_t         kwin;         // last kwin symbols packed, B bits each, last symbol lowest
 };
 
 constexpr uint32_t kStageWaitPolls = 1u << 22;   // default PackArgs::wait_polls

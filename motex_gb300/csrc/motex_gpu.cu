@@ -358,7 +358,9 @@ int sort_factors ( Job * j, uint32_t n, uint32_t ** idx_out, const uint32_t ** k
     uint32_t *kin = key0, *kout = key1, *iin = idx0, *iout = idx1;
     for ( uint32_t ch = 0; ch < nchunk; ++ch )
     {
-        MTX_LAUNCH ( k_gather_key, blocks_for ( n, 256 ), 256, iin, n, dptr<uint8_t> ( j, S_CODES ), l, B, 32 * ch, kin );
+        // chunk 0 (the last symbols) came with the packing, in factor order
+        if ( ch > 0 )
+            MTX_LAUNCH ( k_gather_key, blocks_for ( n, 256 ), 256, iin, n, dptr<uint8_t> ( j, S_CODES ), l, B, 32 * ch, kin );
         const uint32_t cbits = std::min<uint32_t> ( 32, bits - 32 * ch );
         for ( uint32_t pass = 0; pass * 8 < cbits; ++pass )
         {
@@ -698,6 +700,15 @@ int stage_pack ( Job * j, bool * need_sync )
     pa.wait_polls = kStageWaitPolls;
     if ( const char * w = getenv ( "MOTEX_PACK_WAIT_POLLS" ) ) pa.wait_polls = ( uint32_t ) strtoul ( w, nullptr, 10 );
     MTX_CUDA ( cudaMemsetAsync ( scalar + 3, 0, 4, st ) );
+    // the factor sort's first key chunk is formed by the packer itself
+    const bool sorting = P.nb_gaps == 0 && ! j->npat && j->nwords > 0;
+    pa.key0 = nullptr;
+    pa.kwin = 0;
+    if ( sorting )
+    {
+        MTX_TRY ( ensure ( j, S_KEY0, j->nwords, &pa.key0 ) );
+        pa.kwin = std::min<uint32_t> ( P.l, 31u / ( uint32_t ) B + 1u );
+    }
     // persistent: 8 CTAs per SM (the register and shared-memory budget allows
     // it), each with two staged tiles in flight
     const uint64_t ntiles = ( j->total + kPackTile - 1 ) / kPackTile;
@@ -705,7 +716,7 @@ int stage_pack ( Job * j, bool * need_sync )
 
     j->structured = P.nb_gaps > 0;
     j->generic = ! j->structured && P.l > 32;
-    if ( ! j->structured && ! j->npat && j->nwords > 0 )
+    if ( sorting )
     {
         uint32_t * idx;
         const uint32_t * keys;

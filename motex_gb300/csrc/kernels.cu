@@ -247,7 +247,7 @@ __device__ __forceinline__ unsigned long long pack_keys ( uint32_t c, unsigned l
  * bit 1 of *a.err if that gives up too) for the copies it had in flight, so
  * none lands in shared memory the CTA no longer owns.
  */
-__global__ void __launch_bounds__ ( kPackThreads ) k_pack ( PackArgs a )
+__global__ void __launch_bounds__ ( kPackThreads, kPackCtasPerSm ) k_pack ( PackArgs a )
 {
     __shared__ __align__ ( 128 ) uint8_t stage[2][kPackTile];
     __shared__ __align__ ( 8 ) uint64_t bar[2];

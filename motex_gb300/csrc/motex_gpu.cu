@@ -709,10 +709,11 @@ int stage_pack ( Job * j, bool * need_sync )
         MTX_TRY ( ensure ( j, S_KEY0, j->nwords, &pa.key0 ) );
         pa.kwin = std::min<uint32_t> ( P.l, 31u / ( uint32_t ) B + 1u );
     }
-    // persistent: 8 CTAs per SM (the register and shared-memory budget allows
-    // it), each with two staged tiles in flight
+    // persistent: kPackCtasPerSm CTAs per SM (the launch bounds give every
+    // one its registers), each with two staged tiles in flight
     const uint64_t ntiles = ( j->total + kPackTile - 1 ) / kPackTile;
-    MTX_LAUNCH ( k_pack, ( unsigned ) std::min<uint64_t> ( ntiles, 8ull * j->ctx->num_sms ), kPackThreads, pa );
+    MTX_LAUNCH ( k_pack, ( unsigned ) std::min<uint64_t> ( ntiles, ( uint64_t ) kPackCtasPerSm * j->ctx->num_sms ),
+                 kPackThreads, pa );
 
     j->structured = P.nb_gaps > 0;
     j->generic = ! j->structured && P.l > 32;

@@ -204,23 +204,25 @@ __device__ __forceinline__ void bulk_copy_g2s ( void * dst, const void * src, ui
                    : "memory" );
 }
 
-// Key of the factor ending at each lane's position (its last `win`
-// symbols, B bits each, the last one lowest): c = this step's codes, pk =
-// the previous step's keys.  Window sizes double per level; a lane below s
-// takes the low s symbols of the previous step's key.
-__device__ __forceinline__ unsigned long long pack_keys ( uint32_t c, unsigned long long pk, uint32_t win, uint32_t B,
-                                                          unsigned long long keymask, int lane )
+// Low 32 bits of the key of the factor ending at each lane's position (its
+// last `win` symbols, B bits each, the last one lowest): c = this step's
+// codes, pk = the previous step's keys.  Window sizes double per level; a
+// lane below s takes the low s symbols of the previous step's key.  Only the
+// low 32 bits are kept at every level: bits shifted past 32 never come back
+// down, so the truncated doubling gives the truncated key (s * B < 32 on
+// every level that runs, since s < win <= 31 / B + 1).
+__device__ __forceinline__ uint32_t pack_keys ( uint32_t c, uint32_t pk, uint32_t win, uint32_t B, int lane )
 {
-    unsigned long long y = c;
+    uint32_t y = c;
     for ( uint32_t s = 1; s < win; s <<= 1 )
     {
-        const unsigned long long cur = __shfl_up_sync ( 0xffffffffu, y, s );
-        const unsigned long long old = __shfl_sync ( 0xffffffffu, pk, ( lane + 32 - ( int ) s ) & 31 );
-        const unsigned long long low = ( 1ull << ( s * B ) ) - 1ull;
-        const unsigned long long src = lane >= ( int ) s ? cur : ( old & low );
-        y = ( y | ( src << ( s * B ) ) ) & keymask;
+        const uint32_t cur = __shfl_up_sync ( 0xffffffffu, y, s );
+        const uint32_t old = __shfl_sync ( 0xffffffffu, pk, ( lane + 32 - ( int ) s ) & 31 );
+        const uint32_t low = ( 1u << ( s * B ) ) - 1u;
+        const uint32_t src = lane >= ( int ) s ? cur : ( old & low );
+        y |= src << ( s * B );
     }
-    return y & keymask;
+    return y;
 }
 
 } // namespace
@@ -321,12 +323,12 @@ __global__ void __launch_bounds__ ( kPackThreads, kPackCtasPerSm ) k_pack ( Pack
         // keys of the block before the warp's first one (its lanes' low
         // windows, the part the doubling reads, need no earlier block)
         const bool want_keys = a.key0 != nullptr;
-        const unsigned long long keymask = ( 1ull << ( a.kwin * ( uint32_t ) a.B ) ) - 1ull;
-        unsigned long long pk = 0;
+        const uint32_t kmask = a.kwin * ( uint32_t ) a.B >= 32 ? 0xffffffffu : ( 1u << ( a.kwin * a.B ) ) - 1u;
+        uint32_t pk = 0;
         if ( want_keys && k0 > 0 )
         {
             const uint64_t pp = ( k0 - 1 ) * 32 + lane;
-            pk = pack_keys ( pp < a.total ? cmap[a.raw[pp]] : 0u, 0ull, a.kwin, a.B, keymask, lane );
+            pk = pack_keys ( pp < a.total ? cmap[a.raw[pp]] : 0u, 0u, a.kwin, a.B, lane ) & kmask;
         }
 #pragma unroll 4
         for ( int i = 0; i < 32; ++i, pos += 32 )
@@ -345,10 +347,10 @@ __global__ void __launch_bounds__ ( kPackThreads, kPackCtasPerSm ) k_pack ( Pack
                 code = cmap[row[i * 32 + lane]];
                 a.codes[pos] = ( uint8_t ) code;
             }
-            unsigned long long key = 0;
+            uint32_t key = 0;
             if ( want_keys )
             {
-                key = pack_keys ( code, pk, a.kwin, a.B, keymask, lane );
+                key = pack_keys ( code, pk, a.kwin, a.B, lane ) & kmask;
                 pk = key;
             }
             if ( pos < a.total )
@@ -362,7 +364,7 @@ __global__ void __launch_bounds__ ( kPackThreads, kPackCtasPerSm ) k_pack ( Pack
                 if ( ! is_short && rel + 1 >= a.l && ( a.npat == 0 || s < a.npat ) )
                 {
                     a.wpos[ws + ( uint32_t ) ( rel + 1 - a.l )] = ( uint32_t ) pos;
-                    if ( want_keys ) a.key0[ws + ( uint32_t ) ( rel + 1 - a.l )] = ( uint32_t ) key;
+                    if ( want_keys ) a.key0[ws + ( uint32_t ) ( rel + 1 - a.l )] = key;
                 }
             }
 #pragma unroll
@@ -507,8 +509,10 @@ __global__ void __launch_bounds__ ( kSortThreads ) k_radix_scatter ( const uint3
     }
     __syncthreads ();
     // pass 1: ranks within the warp's items of each digit, in input order
+    // (keys and ranks in registers -- two 16-bit ranks per register; the
+    // values are read in pass 2, so each is still read once)
     const uint32_t lt = lanemask_lt ();
-    uint32_t key[ROUNDS], val[ROUNDS], loc[ROUNDS];
+    uint32_t key[ROUNDS], loc[ROUNDS / 2];
     uint32_t * wh = s_wh[warp];
 #pragma unroll
     for ( int r = 0; r < ROUNDS; ++r )
@@ -516,14 +520,15 @@ __global__ void __launch_bounds__ ( kSortThreads ) k_radix_scatter ( const uint3
         const uint32_t li = warp * PER_WARP + r * 32 + lane;
         const bool valid = li < tn;
         key[r] = valid ? keys_in[base + li] : 0u;
-        val[r] = valid ? vals_in[base + li] : 0u;
         const uint32_t d = valid ? ( ( key[r] >> shift ) & 255u ) : ( 256u + lane );
         const uint32_t peers = __match_any_sync ( full, d );
         const uint32_t before = valid ? wh[d] : 0u;
         __syncwarp ();
         if ( valid && ( peers & lt ) == 0 ) wh[d] = before + __popc ( peers );
         __syncwarp ();
-        loc[r] = before + __popc ( peers & lt );
+        const uint32_t rank = before + __popc ( peers & lt );            // < 512
+        if ( r & 1 ) loc[r >> 1] |= rank << 16;
+        else loc[r >> 1] = rank;
     }
     __syncthreads ();
     // per digit: warp offsets (exclusive over warps) and the tile count, then
@@ -561,9 +566,9 @@ __global__ void __launch_bounds__ ( kSortThreads ) k_radix_scatter ( const uint3
         if ( li < tn )
         {
             const uint32_t d = ( key[r] >> shift ) & 255u;
-            const uint32_t pos = s_start[d] + wh[d] + loc[r];
+            const uint32_t pos = s_start[d] + wh[d] + ( ( loc[r >> 1] >> ( ( r & 1 ) * 16 ) ) & 0xffffu );
             s_key[pos] = key[r];
-            s_val[pos] = val[r];
+            s_val[pos] = vals_in[base + li];
         }
     }
     __syncthreads ();

@@ -271,9 +271,15 @@ def dp_kernel_name(wl):
     """The engine's default DP kernel for the workload (bit planes B from the
     symbols present; the autotuner may pick another shape of the same kernel)."""
     if wl.boxes:
-        if len(wl.boxes) > 1:
-            return "k_dp_structN"
-        return "k_dp_struct1_swar_blk" if wl.d == 1 else "k_dp_struct1_hd"
+        lens = [wl.k] + [b[2] for b in wl.boxes]
+        if len(wl.boxes) == 1 and max(lens) <= 32 and wl.boxes[0][1] + wl.boxes[0][2] <= 31:
+            return "k_dp_struct1_swar_blk" if wl.d == 1 else "k_dp_struct1_hd"
+        # the block form packs every box row of a lane in one register
+        span = sum(b[1] - b[0] for b in wl.boxes) + 1
+        fits = (sum(x + 1 for x in lens) - 1 <= 32) if wl.d == 1 else (len(lens) * max(lens) <= 32)
+        if len(lens) <= 4 and max(lens) <= 32 and span <= 17 and fits:
+            return "k_dp_structN_blk"
+        return "k_dp_structN"
     if wl.k > 32:
         return "k_dp_generic"
     sigma = len(set("".join(wl.seqs)))

@@ -581,6 +581,9 @@ def run_gpu(args, rank, world, local_rank):
     if rank == 0 and not args.no_extras and args.scale == 1.0:
         extras["batched_vs_plain"] = batched_vs_plain(native, ctx)
         extras["serving"] = serving(native, nreq=args.serve_requests)
+        # a rate both arms sustain (the one-at-a-time arm serves about 90
+        # requests/s): latency is then service time, not queue growth
+        extras["serving"]["at_40hz"] = serving(native, nreq=max(100, args.serve_requests * 2 // 5), rate_hz=40.0)
     out = {
         "metric": "GCUPS (reference DP cell updates per second), whole-set word-based motif extraction",
         "value": round(value, 2), "unit": "GCUPS", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,

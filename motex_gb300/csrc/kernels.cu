@@ -521,7 +521,16 @@ __global__ void __launch_bounds__ ( kSortThreads ) k_radix_scatter ( const uint3
         const bool valid = li < tn;
         key[r] = valid ? keys_in[base + li] : 0u;
         const uint32_t d = valid ? ( ( key[r] >> shift ) & 255u ) : ( 256u + lane );
-        const uint32_t peers = __match_any_sync ( full, d );
+        // lanes with this lane's digit: eight ballots over the digit bits
+        // (and the invalid lanes, whose d >= 256, kept out by the valid vote)
+        const uint32_t vb = __ballot_sync ( full, valid );
+        uint32_t peers = valid ? vb : ( 1u << lane );
+#pragma unroll
+        for ( int b = 0; b < 8; ++b )
+        {
+            const uint32_t bal = __ballot_sync ( full, ( d >> b ) & 1u );
+            peers &= ( ( d >> b ) & 1u ) ? bal : ~bal;
+        }
         const uint32_t before = valid ? wh[d] : 0u;
         __syncwarp ();
         if ( valid && ( peers & lt ) == 0 ) wh[d] = before + __popc ( peers );

@@ -614,11 +614,13 @@ __global__ void k_heads ( const uint32_t * __restrict__ idx, const uint32_t * __
     head[i] = h;
 }
 
+// Grid-stride (a few CTAs per SM): heads are sparse on repetitive inputs,
+// where one thread per flag made the launch itself the cost.
 __global__ void k_unique ( const uint32_t * __restrict__ idx, const uint8_t * __restrict__ head,
                            const uint32_t * __restrict__ pref, uint32_t n, uint32_t * __restrict__ uniq_pos )
 {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if ( i < n && head[i] ) uniq_pos[pref[i]] = idx[i];
+    for ( uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x )
+        if ( head[i] ) uniq_pos[pref[i]] = idx[i];
 }
 
 /*
@@ -695,16 +697,19 @@ __global__ void k_finalize ( FinalizeArgs a )
     }
 }
 
+// Grid-stride like k_unique (marks are sparse).
 __global__ void k_compact ( const uint8_t * __restrict__ mark, const uint32_t * __restrict__ pref, uint32_t n,
                             const uint32_t * __restrict__ rec_u, const uint32_t * __restrict__ rec_v,
                             uint32_t * __restrict__ out )
 {
-    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-    if ( p >= n || ! mark[p] ) return;
-    const uint32_t j = pref[p];
-    out[3 * ( size_t ) j + 0] = p;
-    out[3 * ( size_t ) j + 1] = rec_u[p];
-    out[3 * ( size_t ) j + 2] = rec_v[p];
+    for ( uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x )
+    {
+        if ( ! mark[p] ) continue;
+        const uint32_t j = pref[p];
+        out[3 * ( size_t ) j + 0] = p;
+        out[3 * ( size_t ) j + 1] = rec_u[p];
+        out[3 * ( size_t ) j + 2] = rec_v[p];
+    }
 }
 
 } // namespace mtx

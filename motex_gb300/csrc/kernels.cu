@@ -214,13 +214,16 @@ __device__ __forceinline__ void bulk_copy_g2s ( void * dst, const void * src, ui
 __device__ __forceinline__ uint32_t pack_keys ( uint32_t c, uint32_t pk, uint32_t win, uint32_t B, int lane )
 {
     uint32_t y = c;
-    for ( uint32_t s = 1; s < win; s <<= 1 )
+#pragma unroll
+    for ( int lv = 0; lv < 5; ++lv )                 // s = 1, 2, 4, 8, 16 while s < win (warp-uniform)
     {
+        const uint32_t s = 1u << lv;
+        if ( s >= win ) break;
         const uint32_t cur = __shfl_up_sync ( 0xffffffffu, y, s );
         const uint32_t old = __shfl_sync ( 0xffffffffu, pk, ( lane + 32 - ( int ) s ) & 31 );
-        const uint32_t low = ( 1u << ( s * B ) ) - 1u;
-        const uint32_t src = lane >= ( int ) s ? cur : ( old & low );
-        y |= src << ( s * B );
+        const uint32_t sb = s * B;
+        const uint32_t src = lane >= ( int ) s ? cur : ( old & ( ( 1u << sb ) - 1u ) );
+        y |= src << sb;
     }
     return y;
 }
@@ -300,14 +303,16 @@ __global__ void __launch_bounds__ ( kPackThreads, kPackCtasPerSm ) k_pack ( Pack
             }
         }
 
-        const uint64_t k0 = t * ( kPackTile / 32 ) + ( uint64_t ) warp * 32;     // first block of this warp
+        // 32-bit positions: inputs are below 2^32 symbols (the host refuses more)
+        const uint32_t total = ( uint32_t ) a.total;
+        const uint32_t k0 = ( uint32_t ) t * ( kPackTile / 32 ) + ( uint32_t ) warp * 32;     // first block of this warp
         // staged row, or after a failed wait the same bytes from global memory
         // (row[i * 32 + lane] is read only for positions below a.total)
-        const uint8_t * row = failed ? a.raw + k0 * 32 : stage[buf] + ( size_t ) warp * 32 * 32;
-        uint64_t pos = k0 * 32 + lane;
+        const uint8_t * row = failed ? a.raw + ( size_t ) k0 * 32 : stage[buf] + ( size_t ) warp * 32 * 32;
+        uint32_t pos = k0 * 32 + lane;
         // sequence of this lane's first position: offs[s] <= pos < offs[s + 1]
         uint32_t s = 0;
-        if ( pos < a.total )
+        if ( pos < total )
         {
             uint32_t lo = 0, hi = a.nseq;
             while ( hi - lo > 1 )
@@ -317,7 +322,7 @@ __global__ void __launch_bounds__ ( kPackThreads, kPackCtasPerSm ) k_pack ( Pack
             }
             s = lo;
         }
-        uint64_t start = a.offs[s], end = a.offs[s + 1];
+        uint32_t start = a.offs[s], end = a.offs[s + 1];
         uint32_t ws = a.wstart[s];
         uint32_t pl[kMaxPlanes] = {}, vm_mine = 0, em_mine = 0;
         // keys of the block before the warp's first one (its lanes' low
@@ -327,15 +332,15 @@ __global__ void __launch_bounds__ ( kPackThreads, kPackCtasPerSm ) k_pack ( Pack
         uint32_t pk = 0;
         if ( want_keys && k0 > 0 )
         {
-            const uint64_t pp = ( k0 - 1 ) * 32 + lane;
-            pk = pack_keys ( pp < a.total ? cmap[a.raw[pp]] : 0u, 0u, a.kwin, a.B, lane ) & kmask;
+            const uint32_t pp = ( k0 - 1 ) * 32 + lane;
+            pk = pack_keys ( pp < total ? cmap[a.raw[pp]] : 0u, 0u, a.kwin, a.B, lane ) & kmask;
         }
 #pragma unroll 4
         for ( int i = 0; i < 32; ++i, pos += 32 )
         {
             uint32_t code = 0;
             bool valid = false, is_end = false;
-            if ( pos < a.total )
+            if ( pos < total )
             {
                 while ( end <= pos )
                 {
@@ -353,9 +358,9 @@ __global__ void __launch_bounds__ ( kPackThreads, kPackCtasPerSm ) k_pack ( Pack
                 key = pack_keys ( code, pk, a.kwin, a.B, lane ) & kmask;
                 pk = key;
             }
-            if ( pos < a.total )
+            if ( pos < total )
             {
-                const uint64_t rel = pos - start;
+                const uint32_t rel = pos - start;
                 const bool is_short = ( end - start ) < a.tml;
                 // pattern mode: sequences below npat are patterns (factors
                 // only), the rest are texts (searched only)
@@ -363,8 +368,8 @@ __global__ void __launch_bounds__ ( kPackThreads, kPackCtasPerSm ) k_pack ( Pack
                 is_end = pos == end - 1;
                 if ( ! is_short && rel + 1 >= a.l && ( a.npat == 0 || s < a.npat ) )
                 {
-                    a.wpos[ws + ( uint32_t ) ( rel + 1 - a.l )] = ( uint32_t ) pos;
-                    if ( want_keys ) a.key0[ws + ( uint32_t ) ( rel + 1 - a.l )] = key;
+                    a.wpos[ws + rel + 1 - a.l] = pos;
+                    if ( want_keys ) a.key0[ws + rel + 1 - a.l] = key;
                 }
             }
 #pragma unroll
@@ -381,7 +386,7 @@ __global__ void __launch_bounds__ ( kPackThreads, kPackCtasPerSm ) k_pack ( Pack
                 em_mine = ew;
             }
         }
-        const uint64_t k = k0 + lane;
+        const uint32_t k = k0 + lane;
         if ( k < a.nblk )
         {
 #pragma unroll

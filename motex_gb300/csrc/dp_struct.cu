@@ -306,26 +306,24 @@ __global__ void __launch_bounds__ ( kDPThreads ) k_dp_struct1_hd ( const StructA
     uint32_t prev[B];
 #pragma unroll
     for ( int b = 0; b < B; ++b ) prev[b] = __ldg ( planes + ( size_t ) b * stride + ch.warm );
-    // packed form: every thread walks the same text positions, so the
-    // replicated windows of a block are built once per warp into its own
-    // double-buffered rows (lane r takes position r; one warp barrier per
-    // block) instead of by every thread; a CTA-wide buffer behind a CTA
-    // barrier measured slower in the two-gap block kernel
-    __shared__ uint32_t s_win[kDPThreads / 32][2][32 * B];
+    // packed form: every thread of the CTA walks the same text positions, so
+    // the replicated windows of a block are built once into shared memory
+    // (double-buffered: one barrier per block) instead of by every thread
+    __shared__ uint32_t s_win[2][32 * B];
     for ( uint32_t kb = ch.warm; kb < ch.end; ++kb )
     {
         uint32_t cur[B];
-        const uint32_t * win = s_win[warp][( kb - ch.warm ) & 1];
+        const uint32_t * win = s_win[( kb - ch.warm ) & 1];
         if constexpr ( PK )
         {
-            uint32_t * w = s_win[warp][( kb - ch.warm ) & 1];
-#pragma unroll
-            for ( int b = 0; b < B; ++b )
+            uint32_t * w = s_win[( kb - ch.warm ) & 1];
+            for ( uint32_t i = threadIdx.x; i < 32u * B; i += kDPThreads )
             {
+                const uint32_t b = i >> 5, r = i & 31u;
                 const uint32_t pw = __ldg ( planes + ( size_t ) b * stride + kb ), cw = __ldg ( planes + ( size_t ) b * stride + kb + 1 );
-                w[b * 32 + lane] = ( __funnelshift_rc ( pw, cw, lane + 1 ) >> ( 32 - L ) ) * rep3;
+                w[i] = ( __funnelshift_rc ( pw, cw, r + 1 ) >> ( 32 - L ) ) * rep3;
             }
-            __syncwarp ();
+            __syncthreads ();
         }
         else
         {

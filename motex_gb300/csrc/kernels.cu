@@ -303,45 +303,94 @@ __global__ void __launch_bounds__ ( kPackThreads, kPackCtasPerSm ) k_pack ( Pack
             }
         }
 
-        // 32-bit positions: inputs are below 2^32 symbols (the host refuses more)
+        // 32-bit positions: inputs are below 2^32 symbols (the host refuses more).
+        // Lane r packs block k = k0 + r, its 32 positions in order: plane,
+        // mask and key bits accumulate in the lane's registers (no ballot, no
+        // shuffle per position), and every row leaves as one coalesced store.
         const uint32_t total = ( uint32_t ) a.total;
         const uint32_t k0 = ( uint32_t ) t * ( kPackTile / 32 ) + ( uint32_t ) warp * 32;     // first block of this warp
-        // staged row, or after a failed wait the same bytes from global memory
-        // (row[i * 32 + lane] is read only for positions below a.total)
-        const uint8_t * row = failed ? a.raw + ( size_t ) k0 * 32 : stage[buf] + ( size_t ) warp * 32 * 32;
-        uint32_t pos = k0 * 32 + lane;
-        // sequence of this lane's first position: offs[s] <= pos < offs[s + 1]
-        uint32_t s = 0;
-        if ( pos < total )
+        const uint32_t k = k0 + lane;
+        const uint32_t p0 = k * 32;
+        const int B = a.B;
+        // phase 1, in two halves of 16 positions (one 16-byte shared load of the
+        // staged row each, or byte loads from global memory after a failed
+        // wait): codes packed four per word and the planes
+        uint32_t cw[8], pl[kMaxPlanes] = {};
+#pragma unroll
+        for ( int h = 0; h < 2; ++h )
         {
+            uint32_t rw[4];
+            if ( ! failed )
+            {
+                const uint4 q = reinterpret_cast<const uint4 *> ( stage[buf] + ( size_t ) warp * 1024 + lane * 32 )[h];
+                rw[0] = q.x; rw[1] = q.y; rw[2] = q.z; rw[3] = q.w;
+            }
+            else
+            {
+#pragma unroll
+                for ( int q = 0; q < 4; ++q ) rw[q] = 0;
+#pragma unroll
+                for ( int j = 0; j < 16; ++j )
+                    if ( p0 + 16 * h + j < total ) rw[j >> 2] |= ( uint32_t ) a.raw[p0 + 16 * h + j] << ( 8 * ( j & 3 ) );
+            }
+#pragma unroll
+            for ( int j = 0; j < 16; ++j )
+            {
+                const int jj = 16 * h + j;
+                const uint32_t c = p0 + jj < total ? cmap[( rw[j >> 2] >> ( 8 * ( j & 3 ) ) ) & 255u] : 0u;
+                if ( ( jj & 3 ) == 0 ) cw[jj >> 2] = c;
+                else cw[jj >> 2] |= c << ( 8 * ( jj & 3 ) );
+#pragma unroll
+                for ( int b = 0; b < kMaxPlanes; ++b ) pl[b] |= ( ( c >> b ) & 1u ) << jj;
+            }
+        }
+        if ( p0 < total )
+        {
+            uint4 * dst = reinterpret_cast<uint4 *> ( a.codes + p0 );          // codes hold total + 64 bytes
+            dst[0] = make_uint4 ( cw[0], cw[1], cw[2], cw[3] );
+            dst[1] = make_uint4 ( cw[4], cw[5], cw[6], cw[7] );
+        }
+        // the first sort key of each factor: its last kwin codes, B bits each,
+        // the last lowest (32 bits kept); the key before the block comes from
+        // the previous lane's block, or for lane 0 from the raw bytes
+        const bool want_keys = a.key0 != nullptr;
+        const uint32_t kwin = a.kwin;
+        const uint32_t kmask = kwin * ( uint32_t ) B >= 32 ? 0xffffffffu : ( 1u << ( kwin * B ) ) - 1u;
+        uint32_t key = 0;
+        if ( want_keys )
+        {
+            uint32_t last = 0;                                   // key at the block's last position
+#pragma unroll
+            for ( int j = 0; j < 32; ++j )
+                if ( j >= 32 - ( int ) kwin ) last = ( last << B ) | ( ( cw[j >> 2] >> ( 8 * ( j & 3 ) ) ) & 255u );
+            key = __shfl_up_sync ( full, last & kmask, 1 );
+            if ( lane == 0 )
+            {
+                key = 0;
+                for ( uint32_t e = kwin - 1; e >= 1; --e )
+                    if ( p0 >= e ) key = ( key << B ) | cmap[a.raw[p0 - e]];
+            }
+        }
+        // phase 2: sequences, masks, factor ends and keys
+        uint32_t vm = 0, em = 0;
+        if ( p0 < total )
+        {
+            // sequence of the block's first position: offs[s] <= p0 < offs[s + 1]
             uint32_t lo = 0, hi = a.nseq;
             while ( hi - lo > 1 )
             {
                 const uint32_t mid = ( lo + hi ) >> 1;
-                if ( a.offs[mid] <= pos ) lo = mid; else hi = mid;
+                if ( a.offs[mid] <= p0 ) lo = mid; else hi = mid;
             }
-            s = lo;
-        }
-        uint32_t start = a.offs[s], end = a.offs[s + 1];
-        uint32_t ws = a.wstart[s];
-        uint32_t pl[kMaxPlanes] = {}, vm_mine = 0, em_mine = 0;
-        // keys of the block before the warp's first one (its lanes' low
-        // windows, the part the doubling reads, need no earlier block)
-        const bool want_keys = a.key0 != nullptr;
-        const uint32_t kmask = a.kwin * ( uint32_t ) a.B >= 32 ? 0xffffffffu : ( 1u << ( a.kwin * a.B ) ) - 1u;
-        uint32_t pk = 0;
-        if ( want_keys && k0 > 0 )
-        {
-            const uint32_t pp = ( k0 - 1 ) * 32 + lane;
-            pk = pack_keys ( pp < total ? cmap[a.raw[pp]] : 0u, 0u, a.kwin, a.B, lane ) & kmask;
-        }
-#pragma unroll 4
-        for ( int i = 0; i < 32; ++i, pos += 32 )
-        {
-            uint32_t code = 0;
-            bool valid = false, is_end = false;
-            if ( pos < total )
+            uint32_t s = lo;
+            uint32_t start = a.offs[s], end = a.offs[s + 1], ws = a.wstart[s];
+#pragma unroll
+            for ( int j = 0; j < 32; ++j )
             {
+                const uint32_t pos = p0 + j;
+                const uint32_t c = ( cw[j >> 2] >> ( 8 * ( j & 3 ) ) ) & 255u;
+                key = ( ( key << B ) | c ) & kmask;
+                if ( pos >= total ) break;
                 while ( end <= pos )
                 {
                     ++s;
@@ -349,51 +398,26 @@ __global__ void __launch_bounds__ ( kPackThreads, kPackCtasPerSm ) k_pack ( Pack
                     end = a.offs[s + 1];
                     ws = a.wstart[s];
                 }
-                code = cmap[row[i * 32 + lane]];
-                a.codes[pos] = ( uint8_t ) code;
-            }
-            uint32_t key = 0;
-            if ( want_keys )
-            {
-                key = pack_keys ( code, pk, a.kwin, a.B, lane ) & kmask;
-                pk = key;
-            }
-            if ( pos < total )
-            {
                 const uint32_t rel = pos - start;
                 const bool is_short = ( end - start ) < a.tml;
                 // pattern mode: sequences below npat are patterns (factors
                 // only), the rest are texts (searched only)
-                valid = ! is_short && rel >= a.vstart && s >= a.npat;
-                is_end = pos == end - 1;
+                vm |= ( uint32_t ) ( ! is_short && rel >= a.vstart && s >= a.npat ) << j;
+                em |= ( uint32_t ) ( pos == end - 1 ) << j;
                 if ( ! is_short && rel + 1 >= a.l && ( a.npat == 0 || s < a.npat ) )
                 {
                     a.wpos[ws + rel + 1 - a.l] = pos;
                     if ( want_keys ) a.key0[ws + rel + 1 - a.l] = key;
                 }
             }
-#pragma unroll
-            for ( int b = 0; b < kMaxPlanes; ++b )
-            {
-                if ( b >= a.B ) break;
-                const uint32_t word = __ballot_sync ( full, ( code >> b ) & 1u );
-                if ( lane == i ) pl[b] = word;
-            }
-            const uint32_t vw = __ballot_sync ( full, valid ), ew = __ballot_sync ( full, is_end );
-            if ( lane == i )
-            {
-                vm_mine = vw;
-                em_mine = ew;
-            }
         }
-        const uint32_t k = k0 + lane;
         if ( k < a.nblk )
         {
 #pragma unroll
             for ( int b = 0; b < kMaxPlanes; ++b )
-                if ( b < a.B ) a.planes[( size_t ) b * a.plane_stride + k + 1] = pl[b];
-            a.vmask[k] = vm_mine;
-            a.emask[k] = em_mine;
+                if ( b < B ) a.planes[( size_t ) b * a.plane_stride + k + 1] = pl[b];
+            a.vmask[k] = vm;
+            a.emask[k] = em;
         }
         __syncthreads ();                            // this buffer may be refilled
     }

@@ -38,7 +38,7 @@ struct PackArgs
 constexpr uint32_t kStageWaitPolls = 1u << 22;   // default PackArgs::wait_polls
 
 constexpr int kPackThreads = 256;              // 8 warps, each packs 32 blocks of 32 positions
-constexpr int kPackCtasPerSm = 5;              // resident CTAs per SM (k_pack's launch bounds)
+constexpr int kPackCtasPerSm = 4;              // resident CTAs per SM (k_pack's launch bounds)
 constexpr uint32_t kPackTile = 8192;           // positions (raw bytes) per staged tile
 
 struct FinalizeArgs

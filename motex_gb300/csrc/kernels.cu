@@ -234,15 +234,17 @@ __device__ __forceinline__ uint32_t pack_keys ( uint32_t c, uint32_t pk, uint32_
  * Packing.  A persistent grid walks tiles of kPackTile raw bytes; each tile
  * is staged into shared memory by one TMA bulk copy (double-buffered: the
  * copy of the CTA's next tile runs while this one is packed).  Warp w of
- * the CTA packs the tile's 32-position blocks 32w .. 32w+31: in step i,
- * lane r takes position 32(k0+i)+r from shared memory (one conflict-free
- * 32-byte row per step), writes its code and its factor-end entry (both
- * coalesced), and the warp forms block k0+i's bit planes, validity and end
- * masks by ballot; lane i keeps them, so every plane and mask row leaves as
- * one coalesced 128-byte store per warp.  With a.key0 set the warp also
- * forms the first radix-sort key of every factor from the codes of its lanes
- * (a shift-or doubling over the warp, the previous step's keys for the
- * lanes below the window), so the sort starts without a gather pass.
+ * the CTA packs the tile's 32-position blocks 32w .. 32w+31, lane r block
+ * 32w+r, its 32 positions in order: the lane reads its 32-byte row of the
+ * staged tile, and its codes, bit planes, validity and end masks (and with
+ * a.key0 set the first radix-sort key of every factor, a shift-or over the
+ * codes) accumulate in registers, so the sort starts without a gather pass.
+ * Codes, planes and masks leave as one store per lane and row (the rows of
+ * a warp's lanes are consecutive).  Factor ends are written block by block
+ * afterwards, lane L the factor ending at position L (the block's first
+ * sequence comes from the lane that packed it), so each store covers 32
+ * consecutive factors; the keys reach those lanes through a per-warp shared
+ * buffer.
  *
  * Failure path: a staging wait that gives up (a.wait_polls polls) sets bit 0
  * of *a.err.  The CTA then issues no further copy and packs the rest of its
@@ -257,6 +259,7 @@ __global__ void __launch_bounds__ ( kPackThreads, kPackCtasPerSm ) k_pack ( Pack
     __shared__ __align__ ( 128 ) uint8_t stage[2][kPackTile];
     __shared__ __align__ ( 8 ) uint64_t bar[2];
     __shared__ uint8_t cmap[256];
+    extern __shared__ uint32_t s_key[];             // kPackKeyWords per warp, with a.key0 only
     for ( int i = threadIdx.x; i < 256; i += blockDim.x ) cmap[i] = a.cmap[i];
     const uint64_t ntiles = ( a.total + kPackTile - 1 ) / kPackTile;
     if ( threadIdx.x == 0 )
@@ -371,8 +374,10 @@ __global__ void __launch_bounds__ ( kPackThreads, kPackCtasPerSm ) k_pack ( Pack
                     if ( p0 >= e ) key = ( key << B ) | cmap[a.raw[p0 - e]];
             }
         }
-        // phase 2: sequences, masks, factor ends and keys
+        // phase 2: sequences, masks and keys of the lane's block in order; the
+        // keys go to the warp's shared buffer (row per block, 33 words: conflict-free)
         uint32_t vm = 0, em = 0;
+        uint32_t s = 0, start = 0, end = 0, ws = 0;
         if ( p0 < total )
         {
             // sequence of the block's first position: offs[s] <= p0 < offs[s + 1]
@@ -382,21 +387,27 @@ __global__ void __launch_bounds__ ( kPackThreads, kPackCtasPerSm ) k_pack ( Pack
                 const uint32_t mid = ( lo + hi ) >> 1;
                 if ( a.offs[mid] <= p0 ) lo = mid; else hi = mid;
             }
-            uint32_t s = lo;
-            uint32_t start = a.offs[s], end = a.offs[s + 1], ws = a.wstart[s];
+            s = lo;
+            start = a.offs[s];
+            end = a.offs[s + 1];
+            ws = a.wstart[s];
+        }
+        const uint32_t s0 = s, start0 = start, end0 = end, ws0 = ws;
+        uint32_t * skey = s_key + warp * kPackKeyWords;
 #pragma unroll
-            for ( int j = 0; j < 32; ++j )
+        for ( int j = 0; j < 32; ++j )
+        {
+            const uint32_t pos = p0 + j;
+            const uint32_t c = ( cw[j >> 2] >> ( 8 * ( j & 3 ) ) ) & 255u;
+            key = ( ( key << B ) | c ) & kmask;
+            if ( want_keys ) skey[lane * 33 + j] = key;
+            if ( pos < total )
             {
-                const uint32_t pos = p0 + j;
-                const uint32_t c = ( cw[j >> 2] >> ( 8 * ( j & 3 ) ) ) & 255u;
-                key = ( ( key << B ) | c ) & kmask;
-                if ( pos >= total ) break;
                 while ( end <= pos )
                 {
                     ++s;
                     start = end;
                     end = a.offs[s + 1];
-                    ws = a.wstart[s];
                 }
                 const uint32_t rel = pos - start;
                 const bool is_short = ( end - start ) < a.tml;
@@ -404,13 +415,38 @@ __global__ void __launch_bounds__ ( kPackThreads, kPackCtasPerSm ) k_pack ( Pack
                 // only), the rest are texts (searched only)
                 vm |= ( uint32_t ) ( ! is_short && rel >= a.vstart && s >= a.npat ) << j;
                 em |= ( uint32_t ) ( pos == end - 1 ) << j;
-                if ( ! is_short && rel + 1 >= a.l && ( a.npat == 0 || s < a.npat ) )
+            }
+        }
+        __syncwarp ();
+        // phase 3: factor ends and keys, block by block: lane L writes the
+        // factor ending at position L of block k0 + i, so each store covers a
+        // run of 32 consecutive factors; the block's first sequence comes from
+        // the lane that packed it
+#pragma unroll 4
+        for ( int i = 0; i < 32; ++i )
+        {
+            const uint32_t pos = ( k0 + i ) * 32 + lane;
+            uint32_t si = __shfl_sync ( full, s0, i ), st = __shfl_sync ( full, start0, i );
+            uint32_t en = __shfl_sync ( full, end0, i ), w = __shfl_sync ( full, ws0, i );
+            if ( pos < total )
+            {
+                while ( en <= pos )
                 {
-                    a.wpos[ws + rel + 1 - a.l] = pos;
-                    if ( want_keys ) a.key0[ws + rel + 1 - a.l] = key;
+                    ++si;
+                    st = en;
+                    en = a.offs[si + 1];
+                    w = a.wstart[si];
+                }
+                const uint32_t rel = pos - st;
+                if ( ( en - st ) >= a.tml && rel + 1 >= a.l && ( a.npat == 0 || si < a.npat ) )
+                {
+                    const uint32_t idx = w + rel + 1 - a.l;
+                    a.wpos[idx] = pos;
+                    if ( want_keys ) a.key0[idx] = skey[i * 33 + lane];
                 }
             }
         }
+        __syncwarp ();
         if ( k < a.nblk )
         {
 #pragma unroll

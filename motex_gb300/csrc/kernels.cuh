@@ -40,6 +40,7 @@ constexpr uint32_t kStageWaitPolls = 1u << 22;   // default PackArgs::wait_polls
 constexpr int kPackThreads = 256;              // 8 warps, each packs 32 blocks of 32 positions
 constexpr int kPackCtasPerSm = 4;              // resident CTAs per SM (k_pack's launch bounds)
 constexpr uint32_t kPackTile = 8192;           // positions (raw bytes) per staged tile
+constexpr int kPackKeyWords = 32 * 33;         // k_pack's per-warp key buffer (dynamic shared memory)
 
 struct FinalizeArgs
 {

@@ -712,8 +712,11 @@ int stage_pack ( Job * j, bool * need_sync )
     // persistent: kPackCtasPerSm CTAs per SM (the launch bounds give every
     // one its registers), each with two staged tiles in flight
     const uint64_t ntiles = ( j->total + kPackTile - 1 ) / kPackTile;
-    MTX_LAUNCH ( k_pack, ( unsigned ) std::min<uint64_t> ( ntiles, ( uint64_t ) kPackCtasPerSm * j->ctx->num_sms ),
-                 kPackThreads, pa );
+    const size_t key_smem = sorting ? sizeof ( uint32_t ) * kPackKeyWords * ( kPackThreads / 32 ) : 0;
+    MTX_CUDA ( cudaFuncSetAttribute ( k_pack, cudaFuncAttributeMaxDynamicSharedMemorySize, ( int ) key_smem ) );
+    k_pack<<<( unsigned ) std::min<uint64_t> ( ntiles, ( uint64_t ) kPackCtasPerSm * j->ctx->num_sms ), kPackThreads,
+             key_smem, j->ctx->st>>> ( pa );
+    MTX_TRY ( check_launch ( j, "k_pack" ) );
 
     j->structured = P.nb_gaps > 0;
     j->generic = ! j->structured && P.l > 32;

@@ -476,8 +476,21 @@ __device__ __forceinline__ void dp_swar_body ( const DPArgs & a, const SwarConst
         const uint32_t Mhs = Pv[i] & Xh & C.NGm1;
         const uint32_t mh = Pv[i] & Xh & C.HB;
         const uint32_t ph = Ph & C.HB;
-        sc[i] = ( ph >> sh ) * C.ONE + sc[i];
-        sc[i] = ( mh >> sh ) * C.NEG1 + sc[i];
+        if constexpr ( NL != 3 )
+        {
+            // ph and mh are disjoint and their top bit is at most 30 (NL = 2:
+            // 2l <= 30; NL = 4: 3(l+1) + l-1 <= 30), so ph - mh is exact as a
+            // signed word and one arithmetic shift gives every field its
+            // +1 / 0 / -1 (a field's borrow cancels against the next field)
+            const int32_t d = ( int32_t ) ( mh * C.NEG1 + ph );
+            sc[i] = ( uint32_t ) ( d >> sh ) * C.ONE + sc[i];
+        }
+        else
+        {
+            // NL = 3 with l = 10 has its top lane's bit l-1 at bit 31
+            sc[i] = ( ph >> sh ) * C.ONE + sc[i];
+            sc[i] = ( mh >> sh ) * C.NEG1 + sc[i];
+        }
         const uint32_t Ph2 = Ph * C.TWO, Mh2 = Mhs * C.TWO;
         Pv[i] = Mh2 | ~( Xv | Ph2 );
         Mv[i] = Ph2 & Xv & C.NG;

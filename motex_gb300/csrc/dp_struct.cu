@@ -440,6 +440,7 @@ struct HSwarConst
     // 1, 2, -1, and -2^(31-p) for the top bit p of each lane, so that
     // (sc * nm + nm) >> 31 = bit p of ~sc
     uint32_t one, two, neg1, nmA, nmB, nmC;
+    uint32_t sd;                    // 1: the top lane ends below bit 31 (score update by one shift)
 };
 
 bool hswar_shape ( const StructArgs & a, HSwarConst * C )
@@ -475,6 +476,7 @@ bool hswar_shape ( const StructArgs & a, HSwarConst * C )
     C->nmA = 0u - ( 1u << ( 31 - ( a.l0 - 1 ) ) );
     C->nmB = 0u - ( 1u << ( 31 - ( oB + a.b1 - 1 ) ) );
     C->nmC = 0u - ( 1u << ( 31 - ( oC + a.b1 - 1 ) ) );
+    C->sd = oC + a.b1 - 1 <= 30;
     return true;
 }
 
@@ -616,7 +618,7 @@ __global__ void __launch_bounds__ ( kDPThreads ) k_dp_struct1_swar ( const Struc
  * append each), with the Myers state reset at sequence ends; phase 2 visits
  * only the positions where a box-1 row hits or a sequence ends.
  */
-template <int B>
+template <int B, bool SD>
 __global__ void __launch_bounds__ ( kDPThreads ) k_dp_struct1_swar_blk ( const StructArgs a, const HSwarConst C )
 {
     extern __shared__ uint32_t smem[];
@@ -713,8 +715,19 @@ __global__ void __launch_bounds__ ( kDPThreads ) k_dp_struct1_swar_blk ( const S
             const uint32_t Mhs = Pv & Xh & C.NGm1;
             const uint32_t mh = Pv & Xh & C.HB;
             const uint32_t ph = Ph & C.HB;
-            sc = ( ph >> sh ) * C.one + sc;
-            sc = ( mh >> sh ) * C.neg1 + sc;
+            if constexpr ( SD )
+            {
+                // ph, mh disjoint with the top bit below 31: ph - mh is exact
+                // as a signed word, one arithmetic shift moves every lane's
+                // +1 / 0 / -1 to its score field
+                const int32_t d = ( int32_t ) ( mh * C.neg1 + ph );
+                sc = ( uint32_t ) ( d >> sh ) * C.one + sc;
+            }
+            else
+            {
+                sc = ( ph >> sh ) * C.one + sc;
+                sc = ( mh >> sh ) * C.neg1 + sc;
+            }
             const uint32_t Ph2 = Ph * C.two, Mh2 = Mhs * C.two;
             Pv = Mh2 | ~( Xv | Ph2 );
             Mv = Ph2 & Xv & C.NG;
@@ -811,8 +824,9 @@ static void launch_struct_b ( const StructArgs & a, bool ed, dim3 grid, size_t s
         {
             // + the per-thread Eq table of the block kernel
             const size_t smem_t = smem + ( size_t ) ( 1 << B ) * kDPThreads * sizeof ( uint32_t );
-            cudaFuncSetAttribute ( k_dp_struct1_swar_blk<B>, cudaFuncAttributeMaxDynamicSharedMemorySize, ( int ) smem_t );
-            k_dp_struct1_swar_blk<B><<<grid, kDPThreads, smem_t, st>>> ( a, C );
+            auto kern = C.sd ? k_dp_struct1_swar_blk<B, true> : k_dp_struct1_swar_blk<B, false>;
+            cudaFuncSetAttribute ( kern, cudaFuncAttributeMaxDynamicSharedMemorySize, ( int ) smem_t );
+            kern<<<grid, kDPThreads, smem_t, st>>> ( a, C );
         }
         else k_dp_struct1_swar<B><<<grid, kDPThreads, smem, st>>> ( a, C );
     }

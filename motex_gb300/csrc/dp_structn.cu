@@ -42,7 +42,7 @@ namespace mtx
 namespace
 {
 
-template <int B, bool ED, int NR>
+template <int B, bool ED, int NR, bool SD>
 __global__ void __launch_bounds__ ( kDPThreads ) k_dp_structN_blk ( const StructNArgs a, const StructNBlk C )
 {
     constexpr int NGAP = NR - 1;
@@ -215,8 +215,18 @@ __global__ void __launch_bounds__ ( kDPThreads ) k_dp_structN_blk ( const Struct
                     const uint32_t Mhs = Pv & Xh & C.NGm1;
                     const uint32_t mh = Pv & Xh & C.HB;
                     const uint32_t ph = Ph & C.HB;
-                    sc = ( ph >> C.s ) * C.one + sc;
-                    sc = ( mh >> C.s ) * C.neg1 + sc;
+                    if constexpr ( SD )
+                    {
+                        // ph, mh disjoint with the top bit below 31: one
+                        // arithmetic shift of ph - mh updates every field
+                        const int32_t d = ( int32_t ) ( mh * C.neg1 + ph );
+                        sc = ( uint32_t ) ( d >> C.s ) * C.one + sc;
+                    }
+                    else
+                    {
+                        sc = ( ph >> C.s ) * C.one + sc;
+                        sc = ( mh >> C.s ) * C.neg1 + sc;
+                    }
                     const uint32_t Ph2 = Ph * C.two, Mh2 = Mhs * C.two;
                     Pv = Mh2 | ~( Xv | Ph2 );
                     Mv = Ph2 & Xv & C.NG;
@@ -365,8 +375,9 @@ bool launch_blk ( const StructNArgs & a, const StructNBlk & C, dim3 grid, cudaSt
 {
     const size_t smem = blk_smem_bytes ( a, C, B, ED, NR );
     if ( smem > 200 * 1024 ) return false;
-    cudaFuncSetAttribute ( k_dp_structN_blk<B, ED, NR>, cudaFuncAttributeMaxDynamicSharedMemorySize, ( int ) smem );
-    k_dp_structN_blk<B, ED, NR><<<grid, kDPThreads, smem, st>>> ( a, C );
+    auto kern = ED && C.sd ? k_dp_structN_blk<B, ED, NR, true> : k_dp_structN_blk<B, ED, NR, false>;
+    cudaFuncSetAttribute ( kern, cudaFuncAttributeMaxDynamicSharedMemorySize, ( int ) smem );
+    kern<<<grid, kDPThreads, smem, st>>> ( a, C );
     return true;
 }
 
@@ -444,6 +455,7 @@ bool structN_blk_shape ( const StructNArgs & a, const uint32_t * h_xoff, bool ed
         C->NG = ~guards;
         C->NGm1 = C->NG & ~C->HB;
         C->s = s;
+        C->sd = C->off[NR - 1] + L[NR - 1] - 1 <= 30;
     }
     else
     {

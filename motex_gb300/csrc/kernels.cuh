@@ -174,6 +174,7 @@ struct StructNBlk
     uint32_t HB, NG, NGm1, K, SC0, s;
     uint32_t off[kStructNBlkMaxRows];            // bit offset of row b's lane
     uint32_t nm[kStructNBlkMaxRows];             // -(2^(31 - top bit of row b)): hit bit by a multiply-add
+    uint32_t sd;                                 // 1: the top lane ends below bit 31 (score update by one shift)
     // Hamming: the rows as lanes of Lmax bits, factors at the top of their lanes
     uint32_t Lmax, rep;
     uint32_t hmask[kStructNBlkMaxRows];

@@ -49,8 +49,14 @@ def consts(l, e, NL, S):
     return dict(HB=HB, NG=NG, NGm1=NG & ~HB & M32, K=K, SC0=SC0, FM=(1 << S) - 1)
 
 
-def swar_counts(pats, text, l, e, S):
-    """Hit counts of NL = len(pats) factors in one register over text."""
+def signed32(x):
+    return x - (1 << 32) if x & (1 << 31) else x
+
+
+def swar_counts(pats, text, l, e, S, one_shift=False):
+    """Hit counts of NL = len(pats) factors in one register over text.
+    one_shift: the score update of the NL = 2, 4 kernels, ph - mh taken as a
+    signed word and moved to the score fields by one arithmetic shift."""
     NL = len(pats)
     C = consts(l, e, NL, S)
     sh = l - 1
@@ -73,7 +79,10 @@ def swar_counts(pats, text, l, e, S):
         Mhs = Pv & Xh & C["NGm1"]
         mh = Pv & Xh & C["HB"]
         ph = Ph & C["HB"]
-        sc = (sc + (ph >> sh) - (mh >> sh)) & M32
+        if one_shift:
+            sc = (sc + (signed32((ph - mh) & M32) >> sh)) & M32
+        else:
+            sc = (sc + (ph >> sh) - (mh >> sh)) & M32
         Ph2, Mh2 = (Ph << 1) & M32, (Mhs << 1) & M32
         Pv = (Mh2 | ~(Xv | Ph2)) & M32
         Mv = Ph2 & Xv & C["NG"]
@@ -96,6 +105,39 @@ def test_packed_lanes_match_sellers(l):
             pats = ["".join(rng.choice(alpha) for _ in range(l)) for _ in range(NL)]
             text = "".join(rng.choice(alpha) for _ in range(150))
             assert swar_counts(pats, text, l, e, S) == [sum(sellers_hits(p, text, e)) for p in pats], (l, e, alpha)
+
+
+@pytest.mark.parametrize("l", [l for l in range(4, 16) if lanes(l, stride(l)) != 3])
+def test_one_shift_score_update_matches_sellers(l):
+    """NL = 2, 4 (the lanes' top bit at most 30): one arithmetic shift of
+    ph - mh gives the same counts as the two shifts."""
+    rng = random.Random(300 + l)
+    S = stride(l)
+    NL = lanes(l, S)
+    assert (NL - 1) * S + l - 1 <= 30
+    for e in range(0, min(l - 1, 5) + 1):
+        for alpha in ("ACGT", "ACDEFGHIKLMNPQRSTVWY"):
+            pats = ["".join(rng.choice(alpha) for _ in range(l)) for _ in range(NL)]
+            text = "".join(rng.choice(alpha) for _ in range(150))
+            assert swar_counts(pats, text, l, e, S, one_shift=True) == \
+                [sum(sellers_hits(p, text, e)) for p in pats], (l, e, alpha)
+
+
+def test_one_shift_fails_when_the_top_lane_reaches_bit_31():
+    """l = 10 packs three lanes with the top one's bit l-1 at bit 31: ph - mh
+    needs 33 bits there, so that layout keeps the two shifts."""
+    l, S = 10, stride(10)
+    NL = lanes(l, S)
+    assert NL == 3 and (NL - 1) * S + l - 1 == 31
+    rng = random.Random(11)
+    bad = 0
+    for _ in range(20):
+        pats = ["".join(rng.choice("ACGT") for _ in range(l)) for _ in range(NL)]
+        text = "".join(rng.choice("ACGT") for _ in range(200))
+        ref = [sum(sellers_hits(p, text, 3)) for p in pats]
+        assert swar_counts(pats, text, l, 3, S) == ref
+        bad += swar_counts(pats, text, l, 3, S, one_shift=True) != ref
+    assert bad > 0
 
 
 def test_narrow_stride_overflows_for_k4():

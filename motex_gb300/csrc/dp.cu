@@ -253,18 +253,26 @@ SwarConst swar_const ( uint32_t l, uint32_t e, int NL )
 {
     SwarConst C {};
     C.S = swar_stride ( l );
+    // hit bit h of the score fields: score + 2^h - (e+1) stays in [0, 2^(h+1))
+    // for every score in [0, l] when 2^h >= l (e < l), so bit h alone tells
+    // score <= e; NL = 2, 3 have room for 6-bit count fields at h
+    uint32_t h = l - 1;
+    if ( NL != 4 )
+        for ( h = 0; ( 1u << h ) < l; ++h ) {}
     uint32_t guards = 0;
     for ( int j = 0; j < NL; ++j )
     {
         const uint32_t o = j * C.S;
         C.HB |= 1u << ( o + l - 1 );
+        C.HQ |= 1u << ( o + h );
         for ( uint32_t g = o + l; g < o + C.S && g < 32; ++g ) guards |= 1u << g;
-        C.K += ( ( 1u << ( l - 1 ) ) - ( e + 1 ) ) << o;
+        C.K += ( ( 1u << h ) - ( e + 1 ) ) << o;
         C.SC0 += l << o;
     }
     C.NG = ~guards;
     C.NGm1 = C.NG & ~C.HB;
-    C.FM = ( 1u << C.S ) - 1u;
+    C.Q = NL != 4 ? h : 0;
+    C.FM = NL != 4 ? 63u : ( 1u << C.S ) - 1u;
     C.ONE = 1u;
     C.TWO = 2u;
     C.NEG1 = ~0u;

@@ -361,8 +361,11 @@ __device__ __forceinline__ bool next_item ( const WorkItem * items, uint32_t nit
  * up is taken without the lanes' top bits).  With those invariants no carry
  * of (Eq&Pv)+Pv and no shifted Ph/Mh bit crosses into the next lane.  The
  * per-lane scores live in bit fields at i*S (each in [0, l]); the hit test
- * adds 2^(l-1)-(e+1) per field and reads bit l-1 of each field.  Hits are
- * counted in per-lane fields and moved to shared memory every 32 positions.
+ * adds 2^h-(e+1) per field and reads bit h of each field (h = ceil(log2 l)
+ * for NL = 2, 3, whose count fields sit at bit h of each lane, so the hit
+ * bits are added where they are; h = l-1 for NL = 4, whose count shifts
+ * them to the lane base).  Hits are counted in per-lane fields and moved to
+ * shared memory every 32 positions.
  * The step is bound by the ALU pipe (logic ops, shifts, adds); its adds and
  * left shifts are written as multiply-adds by runtime constants so that they
  * issue on the otherwise idle FMA pipe.
@@ -505,13 +508,19 @@ __device__ __forceinline__ void dp_swar_body ( const DPArgs & a, const SwarConst
     const uint32_t lane = tid & 31, wid = tid >> 5;
     const uint32_t * my_eq = s_eq + tid;
     const uint32_t * my_hi = s_hi + tid;
-    auto count = [&] ( int i ) { cnt[i] = ( ( ~sc[i] & C.HB ) >> sh ) * C.ONE + cnt[i]; };
+    // NL = 2, 3: hit bits added where they are (count fields at C.Q of each
+    // lane); NL = 4: shifted to the lane base
+    constexpr bool HIT_IN_PLACE = NL != 4;
+    auto count = [&] ( int i ) {
+        if constexpr ( HIT_IN_PLACE ) cnt[i] = ( ~sc[i] & C.HQ ) * C.ONE + cnt[i];
+        else cnt[i] = ( ( ~sc[i] & C.HQ ) >> sh ) * C.ONE + cnt[i];
+    };
     auto drain = [&] () {                           // register fields -> shared counters
 #pragma unroll
         for ( int i = 0; i < W; ++i )
         {
 #pragma unroll
-            for ( int j = 0; j < NL; ++j ) s_cnt[( i * NL + j ) * kDPThreads + tid] += ( cnt[i] >> ( j * C.S ) ) & C.FM;
+            for ( int j = 0; j < NL; ++j ) s_cnt[( i * NL + j ) * kDPThreads + tid] += ( cnt[i] >> ( j * C.S + C.Q ) ) & C.FM;
             cnt[i] = 0;
         }
     };
@@ -586,7 +595,7 @@ __device__ __forceinline__ void dp_swar_body ( const DPArgs & a, const SwarConst
                     for ( int i = 0; i < W; ++i )
                     {
                         step_eq ( i, TAB ? lo[i * kDPThreads] : ( lo[i * kDPThreads] & hi[i * kDPThreads] ) );
-                        hacc |= ~sc[i] & C.HB;
+                        hacc |= ~sc[i] & C.HQ;
                     }
                 }
                 if ( hacc )

@@ -223,10 +223,16 @@ struct SwarConst
     uint32_t HB;     // bit l-1 of every lane
     uint32_t NG;     // all bits but the guards
     uint32_t NGm1;   // NG without the lanes' top bits
-    uint32_t K;      // per field 2^(l-1) - (e+1)
+    uint32_t K;      // per field 2^h - (e+1): bit h of score + K is clear exactly on a hit
     uint32_t SC0;    // per field score l
     uint32_t S;      // lane stride
-    uint32_t FM;     // field mask (S bits)
+    uint32_t FM;     // count field mask
+    // edit distance: the hit bit h of every lane's score field, and the
+    // offset of the count fields in the lanes.  NL = 2, 3: h = ceil(log2 l),
+    // and the per-step count adds the hit bits where they are (count fields
+    // of 6 bits at h); NL = 4 (too narrow for that): h = l-1, and the count
+    // shifts the hit bits to the lane base
+    uint32_t HQ, Q;
     uint32_t REP;    // Hamming lanes: sum of 2^(j*l), replicates an l-bit window into every lane
     // Multipliers of the edit-distance step, kernel parameters so that the
     // compiler cannot fold them: x * ONE + y, x * TWO and x * NEG1 + y run as

@@ -3,7 +3,8 @@ motex_gb300/csrc/dp_body.cuh, constants from swar_const in dp.cu) restated
 bit for bit in 32-bit arithmetic and checked against a Sellers DP column on
 random factors and texts: NL factors share a register in lanes of
 S = max(l+1, 6) bits with guard bits above each lane, scores held as
-score + K per field, hit counts in S-bit fields drained every 32 positions.
+score + K per field with the hit flag at bit h, hit counts drained every 32
+positions.
 The same check with the narrower stride S = l+1 fails for k = 4 (a block of
 32 hits overflows a 5-bit count field into the next lane), which is how that
 layout bug was found."""
@@ -37,16 +38,22 @@ def lanes(l, S):
 
 
 def consts(l, e, NL, S):
-    HB = K = SC0 = guards = 0
+    """swar_const: hit bit h = ceil(log2 l) of each score field and 6-bit
+    count fields at h for NL = 2, 3; h = l-1 and S-bit count fields at the
+    lane base for NL = 4."""
+    h = l - 1 if NL == 4 else (l - 1).bit_length()
+    HB = HQ = K = SC0 = guards = 0
     for j in range(NL):
         o = j * S
         HB |= 1 << (o + l - 1)
+        HQ |= 1 << (o + h)
         for g in range(o + l, min(o + S, 32)):
             guards |= 1 << g
-        K += ((1 << (l - 1)) - (e + 1)) << o
+        K += ((1 << h) - (e + 1)) << o
         SC0 += l << o
     NG = ~guards & M32
-    return dict(HB=HB, NG=NG, NGm1=NG & ~HB & M32, K=K, SC0=SC0, FM=(1 << S) - 1)
+    return dict(HB=HB, HQ=HQ, NG=NG, NGm1=NG & ~HB & M32, K=K, SC0=SC0, Q=0 if NL == 4 else h,
+                FM=(1 << S) - 1 if NL == 4 else 63)
 
 
 def signed32(x):
@@ -86,10 +93,11 @@ def swar_counts(pats, text, l, e, S, one_shift=False):
         Ph2, Mh2 = (Ph << 1) & M32, (Mhs << 1) & M32
         Pv = (Mh2 | ~(Xv | Ph2)) & M32
         Mv = Ph2 & Xv & C["NG"]
-        cnt = (cnt + (((~sc & M32) & C["HB"]) >> sh)) & M32
+        hits = (~sc & M32) & C["HQ"]
+        cnt = (cnt + (hits if NL != 4 else hits >> sh)) & M32   # NL = 2, 3: added in place
         if k % 32 == 31 or k == len(text) - 1:               # drain per 32-position block
             for j in range(NL):
-                counts[j] += (cnt >> (j * S)) & C["FM"]
+                counts[j] += (cnt >> (j * S + C["Q"])) & C["FM"]
             cnt = 0
     return counts
 
@@ -100,7 +108,8 @@ def test_packed_lanes_match_sellers(l):
     S = stride(l)
     NL = lanes(l, S)
     assert (NL - 1) * S + l <= 32
-    for e in range(0, min(l - 1, 5) + 1):
+    # e = l - 1: nearly every position is a hit, 32 per block fill a count field
+    for e in sorted(set(range(0, min(l - 1, 5) + 1)) | {l - 1}):
         for alpha in ("ACGT", "ACDEFGHIKLMNPQRSTVWY"):
             pats = ["".join(rng.choice(alpha) for _ in range(l)) for _ in range(NL)]
             text = "".join(rng.choice(alpha) for _ in range(150))

@@ -286,9 +286,25 @@ def dp_kernel_name(wl):
     B = max(2, (sigma - 1).bit_length())
     if wl.d == 1 and 4 <= wl.k <= 15:
         return f"k_dp_swar_ed (NL={min(4, 33 // (wl.k + 1))})"
+    if wl.d == 0 and B <= 3 and 5 <= wl.k <= 12 and wl.e <= 3:
+        return "k_dp_hclr (NL=2)"
     if wl.d == 0 and B >= 3 and 6 <= wl.k <= 16:
         return f"k_dp_hswar (NL={32 // wl.k})"
     return "k_dp_fast"
+
+
+def tuned_kernel_name(wl, shape):
+    """The DP kernel of an autotuner entry (W, NL, UR): a negative NL is the
+    guarded-lane Hamming form, NL > 1 a packed form, NL = 1 one factor per
+    register."""
+    W, NL, UR = shape
+    if NL < 0:
+        name = f"k_dp_hclr (NL={-NL})"
+    elif NL > 1:
+        name = f"k_dp_swar_ed (NL={NL})" if wl.d == 1 else f"k_dp_hswar (NL={NL})"
+    else:
+        name = "k_dp_fast"
+    return name + " W=%d NL=%d UR=%d" % (W, abs(NL), UR)
 
 
 def c_level_calls(native, ctx, jobs):
@@ -559,7 +575,7 @@ def run_gpu(args, rank, world, local_rank):
         sigma = len(set("".join(wl.seqs)))
         shape = native.tune_lookup(max(2, (sigma - 1).bit_length()), wl.k, wl.e, wl.d)
         if shape:
-            kernel += " W=%d NL=%d UR=%d" % shape
+            kernel = tuned_kernel_name(wl, shape)
     roofline = {"bound": "int32_alu", "kernel": kernel, "achieved": round(achieved, 3),
                 "peak": round(iadd, 3), "unit": "Tops/s", "frac": round(achieved / iadd, 4) if iadd else None,
                 "peak_source": "measured int32 add throughput, all pipes (motex_probe_int_peak), same run",
@@ -572,8 +588,9 @@ def run_gpu(args, rank, world, local_rank):
     ex = executed_record(args.workload)
     if ex:
         roofline["executed"] = ex
-    if wl.d == 0 and not wl.boxes and dp_s > 0 and popc:
-        # plain Hamming runs one population count per cell: its second roof
+    if wl.d == 0 and not wl.boxes and dp_s > 0 and popc and not kernel.startswith("k_dp_hclr"):
+        # plain Hamming runs one population count per cell (the guarded-lane
+        # form none): its second roof
         popc_rate = first.unique_words * total_pos / dp_s / 1e12
         roofline.update(popc_achieved=round(popc_rate, 3), popc_frac=round(popc_rate / popc, 4))
 

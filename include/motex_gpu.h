@@ -256,9 +256,11 @@ uint64_t motex_ctx_launches ( const motex_ctx * ctx );
  * autotuner holds for the key (bit planes B, factor length l, errors e,
  * distance d) -- register words per thread W, factors per register NL,
  * block unroll UR -- from tuning done in this process or read from the file
- * MOTEX_TUNE_CACHE names (one "B l e d W NL UR" line per entry; lines naming
- * a shape the kernels do not implement are ignored).  MOTEX_ENOTFOUND if the
- * key has no entry.  Host-only: needs no GPU.
+ * MOTEX_TUNE_CACHE names (one "B l e d W NL UR F" line per entry, F the
+ * Hamming form and 0 when absent; lines naming a shape the kernels do not
+ * implement are ignored).  A negative NL reports the popc-free Hamming form:
+ * -NL factors per register in guarded lanes.  MOTEX_ENOTFOUND if the key has
+ * no entry.  Host-only: needs no GPU.
  */
 int motex_tune_lookup ( int B, uint32_t l, uint32_t e, uint32_t d, int * W, int * NL, int * UR );
 

@@ -27,7 +27,7 @@ LIB = os.path.join(PKG, "lib")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off",
               "--expt-relaxed-constexpr", "-I" + INC, "-I" + CSRC]
-CU_SOURCES = ["kernels.cu", "dp.cu", "dp_persist.cu", "dp_struct.cu", "dp_structn.cu", "mini.cu", "motex_gpu.cu", "probe.cu", "no_alloc.cu", "server.cu"]
+CU_SOURCES = ["kernels.cu", "dp.cu", "dp_hclr.cu", "dp_persist.cu", "dp_struct.cu", "dp_structn.cu", "mini.cu", "motex_gpu.cu", "probe.cu", "no_alloc.cu", "server.cu"]
 HEADERS = ["common.cuh", "kernels.cuh", "dp_body.cuh"]
 
 

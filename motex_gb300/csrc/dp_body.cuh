@@ -687,8 +687,22 @@ __device__ __forceinline__ void dp_swar_body ( const DPArgs & a, const SwarConst
  * lane a masked popc.  Hit counts live in l-bit register fields (l >= 6
  * holds a 32-position block), drained to shared memory per block like the
  * edit-distance SWAR body.
+ *
+ * E >= 0 (e = E <= 3): the popc-free form.  Lanes of l bits with a guard
+ * bit above each (lane j at bits [j*S, j*S+l), S = l+1, guard bit j*S+l),
+ * the guards set in the mismatch word x by plane 0 of the factor register.
+ * E times, x = (x & (x - L)) | G clears the lowest set bit of every lane
+ * (L: the lanes' bit 0; a lane already zero borrows from its own guard,
+ * which the OR sets again, so no borrow crosses a lane).  Then the lane has
+ * at most E mismatches exactly when it is zero, and x - L clears its guard
+ * bit exactly then: the hits are ~(x - L) & G, added where they are into
+ * 6-bit count fields at the guard bits.  Per register: B-1 logic ops for x,
+ * one per clear and one for the hits on the ALU pipe; the subtractions and
+ * the count add are multiply-adds (FMA pipe); no popc.  C holds S = l+1,
+ * HB = the guard bits G, K = -L, REP = sum 2^(j*S), Q = l (count field
+ * offset in a lane) and FM = 63.
  */
-template <int B, int NL, int W, int UR>
+template <int B, int NL, int W, int UR, int E = -1>
 __device__ __forceinline__ void dp_hswar_body ( const DPArgs & a, const SwarConst & C, uint32_t tile, uint32_t chunk )
 {
     extern __shared__ uint32_t smem[];
@@ -716,6 +730,7 @@ __device__ __forceinline__ void dp_hswar_body ( const DPArgs & a, const SwarCons
 #pragma unroll
                 for ( int b = 0; b < B; ++b ) fp[i][b] |= ( __ldg ( a.wplanes32 + ( size_t ) b * a.U + w ) >> down ) << ( j * C.S );
         }
+        if constexpr ( E >= 0 ) fp[i][0] |= C.HB;                // guard bits: x has them set
     }
     uint32_t cnt[W];
 #pragma unroll
@@ -730,9 +745,18 @@ __device__ __forceinline__ void dp_hswar_body ( const DPArgs & a, const SwarCons
         uint32_t x = fp[i][0] ^ Y[0];
 #pragma unroll
         for ( int b = 1; b < B; ++b ) x |= fp[i][b] ^ Y[b];
+        if constexpr ( E >= 0 )
+        {
 #pragma unroll
-        for ( int j = 0; j < NL; ++j )
-            if ( __popc ( x & ( C.FM << ( j * C.S ) ) ) <= e ) cnt[i] += 1u << ( j * C.S );
+            for ( int c = 0; c < E; ++c ) x = ( x & ( x * C.ONE + C.K ) ) | C.HB;
+            cnt[i] = ( ~( x * C.ONE + C.K ) & C.HB ) * C.ONE + cnt[i];
+        }
+        else
+        {
+#pragma unroll
+            for ( int j = 0; j < NL; ++j )
+                if ( __popc ( x & ( C.FM << ( j * C.S ) ) ) <= e ) cnt[i] += 1u << ( j * C.S );
+        }
     };
     // the replicated windows of a block (32 positions x B planes) are the same
     // for every thread: built once per CTA into shared memory, double-buffered
@@ -748,7 +772,7 @@ __device__ __forceinline__ void dp_hswar_body ( const DPArgs & a, const SwarCons
         for ( int i = 0; i < W; ++i )
         {
 #pragma unroll
-            for ( int j = 0; j < NL; ++j ) s_cnt[( i * NL + j ) * kDPThreads + tid] += ( cnt[i] >> ( j * C.S ) ) & C.FM;
+            for ( int j = 0; j < NL; ++j ) s_cnt[( i * NL + j ) * kDPThreads + tid] += ( cnt[i] >> ( j * C.S + C.Q ) ) & C.FM;
             cnt[i] = 0;
         }
     };

@@ -247,6 +247,13 @@ SwarConst swar_const ( uint32_t l, uint32_t e, int NL );
 int hswar_lanes ( uint32_t l );
 SwarConst hswar_const ( uint32_t l, int NL );
 bool launch_dp_hswar ( const DPArgs & a, int B, int NL, int W, int UR, dim3 grid, cudaStream_t st );
+// Popc-free Hamming for e <= kHclrMaxE: two factors of l bits per register in
+// guarded lanes (5 <= l <= 12), mismatches counted by clearing each lane's
+// lowest set bit e times (dp_hclr.cu); unroll 4.
+constexpr uint32_t kHclrMaxE = 3;
+int hclr_lanes ( uint32_t l );
+SwarConst hclr_const ( uint32_t l );
+bool launch_dp_hclr ( const DPArgs & a, int B, int NL, int W, dim3 grid, cudaStream_t st );
 // Register words per thread of the packed kernels when the shape is not tuned
 // (batched jobs, persistent launches, the default of an untuned job): with
 // B = 4, 5 the split Eq table leaves room for enough CTAs per SM only at

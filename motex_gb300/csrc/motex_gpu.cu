@@ -90,6 +90,7 @@ struct DPTune
     int W = 8;     // register words per thread
     int NL = 1;    // factors per register word
     int UR = 8;    // unroll of the 32-position block
+    int F = 0;     // Hamming form: 1 = guarded lanes with lowest-bit clears (no popc)
 };
 
 } // namespace
@@ -387,23 +388,39 @@ int sort_factors ( Job * j, uint32_t n, uint32_t ** idx_out, const uint32_t ** k
  * 32-position text block (UR, bounded to keep the loop in the instruction
  * cache).  MOTEX_DP_W / MOTEX_DP_UR / MOTEX_DP_SWAR=0 override the choice.
  */
+bool hclr_eligible ( uint32_t l, uint32_t e ) { return e <= kHclrMaxE && hclr_lanes ( l ) == 2; }
+
 DPTune choose_tune ( Job * j, uint32_t U, bool ed, bool generic )
 {
     DPTune t;
     if ( generic ) { t.W = 1; t.NL = 1; t.UR = 32; return t; }
     t.NL = ed ? swar_lanes ( j->prm.l ) : ( j->B >= 3 ? hswar_lanes ( j->prm.l ) : 1 );
+    // Hamming with e <= 3 and 5 <= l <= 12 over 2-3 bit planes: the popc-free
+    // guarded-lane form by default (measured on GB300: config 1 DP 0.235 ->
+    // 0.201 ms; with 4-5 planes the three-lane popc form stays ahead, the
+    // autotuner tries both); MOTEX_DP_CLEAR=0 keeps the popc forms
+    const char * clr = getenv ( "MOTEX_DP_CLEAR" );
+    if ( ! ed && j->B <= 3 && hclr_eligible ( j->prm.l, j->prm.e ) && ! ( clr && atoi ( clr ) == 0 ) )
+    {
+        t.NL = hclr_lanes ( j->prm.l );
+        t.F = 1;
+    }
     const uint32_t groups = ( U + t.NL - 1 ) / t.NL;
     t.W = groups >= ( uint32_t ) j->ctx->num_sms * kDPThreads * 8 ? 8 : 4;
     if ( t.NL > 1 ) t.W = std::min ( t.W, swar_default_w ( j->B ) );
     t.UR = ed ? 8 : 4;             // measured on GB300: Hamming prefers the shorter body
     if ( const char * e = getenv ( "MOTEX_DP_SWAR" ) )
-        if ( atoi ( e ) == 0 ) t.NL = 1;
+        if ( atoi ( e ) == 0 )
+        {
+            t.NL = 1;
+            t.F = 0;
+        }
     if ( const char * e = getenv ( "MOTEX_DP_W" ) )
         if ( atoi ( e ) == 4 || atoi ( e ) == 8 ) t.W = atoi ( e );
     if ( const char * e = getenv ( "MOTEX_DP_UR" ) )
     {
         const int v = atoi ( e );
-        if ( v == 4 || v == 8 || ( v == 32 && t.NL == 1 ) ) t.UR = v;
+        if ( ( v == 4 || v == 8 || ( v == 32 && t.NL == 1 ) ) && ! ( t.F && v != 4 ) ) t.UR = v;
     }
     return t;
 }
@@ -446,6 +463,8 @@ bool tune_entry_valid ( const TuneKey & k, const DPTune & t )
 {
     if ( k.B < 2 || k.B > kMaxPlanes || k.l < 1 || k.l > 32 || k.e >= k.l || k.d > 1 ) return false;
     if ( t.W != 4 && t.W != 8 ) return false;
+    if ( t.F != 0 )                                         // guarded-lane Hamming
+        return t.F == 1 && k.d == 0 && hclr_eligible ( k.l, k.e ) && t.NL == hclr_lanes ( k.l ) && t.UR == 4;
     const int packed = k.d == 1 ? swar_lanes ( k.l ) : ( k.B >= 3 ? hswar_lanes ( k.l ) : 1 );
     if ( t.NL != 1 && ( t.NL != packed || packed < 2 ) ) return false;
     if ( t.UR != 4 && t.UR != 8 && ! ( t.UR == 32 && t.NL == 1 ) ) return false;
@@ -453,9 +472,10 @@ bool tune_entry_valid ( const TuneKey & k, const DPTune & t )
     return true;
 }
 
-// Entries of the MOTEX_TUNE_CACHE file, one "B l e d W NL UR" line each; a
-// line that does not parse or names a shape the kernels do not implement is
-// skipped (a later valid line for the same key wins).
+// Entries of the MOTEX_TUNE_CACHE file, one "B l e d W NL UR F" line each (F,
+// the Hamming form, may be absent: 0); a line that does not parse or names a
+// shape the kernels do not implement is skipped (a later valid line for the
+// same key wins).
 void tune_load_locked ()
 {
     if ( g_tune_loaded ) return;
@@ -470,8 +490,9 @@ void tune_load_locked ()
         TuneKey k;
         DPTune t;
         char extra;
-        if ( sscanf ( line, "%d %u %u %u %d %d %d %c", &k.B, &k.l, &k.e, &k.d, &t.W, &t.NL, &t.UR, &extra ) != 7 )
-            continue;
+        const int n = sscanf ( line, "%d %u %u %u %d %d %d %d %c", &k.B, &k.l, &k.e, &k.d, &t.W, &t.NL, &t.UR, &t.F, &extra );
+        if ( n == 7 ) t.F = 0;
+        else if ( n != 8 ) continue;
         if ( tune_entry_valid ( k, t ) ) g_tune[k] = t;
     }
     fclose ( f );
@@ -484,7 +505,7 @@ void tune_store_locked ( const TuneKey & k, const DPTune & t )
     if ( ! path || ! *path ) return;
     if ( FILE * f = fopen ( path, "a" ) )
     {
-        fprintf ( f, "%d %u %u %u %d %d %d\n", k.B, k.l, k.e, k.d, t.W, t.NL, t.UR );
+        fprintf ( f, "%d %u %u %u %d %d %d %d\n", k.B, k.l, k.e, k.d, t.W, t.NL, t.UR, t.F );
         fclose ( f );
     }
 }
@@ -502,6 +523,7 @@ bool tune_lookup ( const TuneKey & k, DPTune * t )
 bool launch_shape ( Job * j, const DPArgs & da, const DPTune & t, dim3 grid )
 {
     const bool ed = j->prm.d == 1;
+    if ( t.F ) return launch_dp_hclr ( da, j->B, t.NL, t.W, grid, j->ctx->st );
     if ( t.NL > 1 )
         return ed ? launch_dp_swar_ed ( da, j->B, t.NL, t.W, t.UR, grid, j->ctx->st )
                   : launch_dp_hswar ( da, j->B, t.NL, t.W, t.UR, grid, j->ctx->st );
@@ -519,9 +541,11 @@ int autotune ( Job * j, DPTune * best )
         for ( int W : { 4, 8 } )
             for ( int UR : { 4, 8 } )
                 if ( ed || NL == 1 || UR == 4 )              // packed Hamming exists with unroll 4 only
-                    cands.push_back ( DPTune { W, NL, UR } );
+                    cands.push_back ( DPTune { W, NL, UR, 0 } );
         if ( NL == 1 ) break;
     }
+    if ( ! ed && hclr_eligible ( j->prm.l, j->prm.e ) )
+        for ( int W : { 4, 8 } ) cands.push_back ( DPTune { W, hclr_lanes ( j->prm.l ), 4, 1 } );
     // probe chunks: consecutive 512-block ranges from the start of the text, no splits
     const uint32_t pblk = std::min<uint32_t> ( j->nblk, kTuneBlocks );
     const uint32_t maxc = std::max<uint32_t> ( 1, std::min<uint32_t> ( 16, j->nblk / pblk ) );
@@ -1094,6 +1118,7 @@ int stage_dp ( Job * j )
     {
         const dim3 grid ( j->ntiles, ( unsigned ) j->chunks.size () );
         ok = j->generic        ? launch_dp_generic ( j->da, j->B, j->nw64, ed, grid, st )
+             : j->tune.F       ? launch_dp_hclr ( j->da, j->B, j->tune.NL, j->tune.W, grid, st )
              : j->tune.NL > 1  ? ( ed ? launch_dp_swar_ed ( j->da, j->B, j->tune.NL, j->tune.W, j->tune.UR, grid, st )
                                         : launch_dp_hswar ( j->da, j->B, j->tune.NL, j->tune.W, j->tune.UR, grid, st ) )
                                : launch_dp_fast ( j->da, j->B, j->tune.W, j->tune.UR, ed, grid, st );
@@ -1527,10 +1552,15 @@ int batch_dp ( motex_ctx * c, std::vector<Job *> & jobs, float * dp_ms )
         DPTune t;
         const bool tuned = ! getenv ( "MOTEX_DP_W" ) && ! getenv ( "MOTEX_DP_UR" ) && ! getenv ( "MOTEX_DP_SWAR" ) &&
                            tune_lookup ( TuneKey { j->B, j->prm.l, j->prm.e, j->prm.d }, &t ) &&
-                           persistent_shape ( Bc, ed, t.NL, t.W, t.UR );
+                           t.F == 0 && persistent_shape ( Bc, ed, t.NL, t.W, t.UR );
         if ( tuned ) j->tune = t;
         else
         {
+            if ( j->tune.F )                        // no persistent guarded-lane kernel: the popc forms
+            {
+                j->tune.F = 0;
+                j->tune.NL = j->B >= 3 ? hswar_lanes ( j->prm.l ) : 1;
+            }
             j->tune.W = ( j->tune.NL > 1 && ed ) ? swar_default_w ( Bc ) : 8;
             j->tune.UR = ( j->tune.NL > 1 ? ( ed ? 8 : 4 ) : ( ed ? 8 : 4 ) );
         }
@@ -2138,7 +2168,7 @@ int motex_tune_lookup ( int B, uint32_t l, uint32_t e, uint32_t d, int * W, int 
     if ( ! tune_lookup ( TuneKey { B, l, e, d }, &t ) )
         return fail ( MOTEX_ENOTFOUND, "no launch shape tuned for B=%d l=%u e=%u d=%u", B, l, e, d );
     *W = t.W;
-    *NL = t.NL;
+    *NL = t.F ? -t.NL : t.NL;                   // negative: guarded lanes, lowest-bit clears
     *UR = t.UR;
     return MOTEX_OK;
 }

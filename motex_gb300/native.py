@@ -135,7 +135,8 @@ class Extraction:
 
 
 def tune_lookup(B: int, l: int, e: int, d: int):
-    """(W, NL, UR) the autotuner holds for the key, or None (host-only)."""
+    """(W, NL, UR) the autotuner holds for the key, or None (host-only); a
+    negative NL is the popc-free Hamming form with -NL guarded lanes."""
     lib = load_library()
     W, NL, UR = C.c_int(), C.c_int(), C.c_int()
     rc = lib.motex_tune_lookup(B, l, e, d, C.byref(W), C.byref(NL), C.byref(UR))

@@ -221,6 +221,74 @@ def test_packed_hamming_needs_six_bit_lanes():
         assert (hswar_counts(pats, text, l, 0) == [hamming_hits(p, text, 0) for p in pats]) == ok, l
 
 
+# ------------------------------- popc-free Hamming: guarded lanes, bit clears
+
+def hclr_counts(pats, text, l, e):
+    """dp_hswar_body with E = e (hclr_const in dp_hclr.cu) restated: two
+    factors of l bits in lanes at 0 and S = l+1 with a guard bit above each,
+    set in the mismatch word; e times x = (x & (x - L)) | G clears each lane's
+    lowest set bit; the hits are ~(x - L) & G (a lane that is zero borrows
+    its guard), added into 6-bit count fields at the guards and drained every
+    32 positions."""
+    NL, S = len(pats), l + 1
+    assert NL == 2 and 5 <= l <= 12 and e <= 3
+    G = sum(1 << (j * S + l) for j in range(NL))
+    L = sum(1 << (j * S) for j in range(NL))
+    codes = {c: i for i, c in enumerate(sorted(set(text) | set("".join(pats))))}
+    nbits = max(1, (len(codes) - 1).bit_length())
+    fp = [0] * nbits
+    for j, p in enumerate(pats):
+        for q, ch in enumerate(p):
+            for b in range(nbits):
+                if (codes[ch] >> b) & 1:
+                    fp[b] |= 1 << (j * S + q)
+    fp[0] |= G
+    cnt, counts = 0, [0] * NL
+    for k in range(len(text)):
+        if k >= l - 1:
+            win = text[k - l + 1:k + 1]
+            x = 0
+            for b in range(nbits):
+                w = sum(((codes[ch] >> b) & 1) << q for q, ch in enumerate(win))
+                x |= fp[b] ^ ((w * L) & M32)                # window copies at 0 and S
+            for _ in range(e):
+                x = ((x & ((x - L) & M32)) | G) & M32
+            cnt = (cnt + (~((x - L) & M32) & G)) & M32
+        if k % 32 == 31 or k == len(text) - 1:
+            for j in range(NL):
+                counts[j] += (cnt >> (j * S + l)) & 63
+            cnt = 0
+    return counts
+
+
+@pytest.mark.parametrize("l", range(5, 13))
+def test_guarded_lane_hamming_matches(l):
+    rng = random.Random(500 + l)
+    for e in range(0, min(3, l - 1) + 1):
+        for alpha in ("ACGT", "ACDEFGHIKLMNPQRSTVWY"):
+            for _ in range(3):
+                pats = ["".join(rng.choice(alpha) for _ in range(l)) for _ in range(2)]
+                text = "".join(rng.choice(alpha) for _ in range(150))
+                # plant both factors with up to e substitutions
+                for p in pats:
+                    a = rng.randint(0, len(text) - l)
+                    occ = list(p)
+                    for q in rng.sample(range(l), rng.randint(0, e)):
+                        occ[q] = rng.choice(alpha)
+                    text = text[:a] + "".join(occ) + text[a + l:]
+                assert hclr_counts(pats, text, l, e) == [hamming_hits(p, text, e) for p in pats], (l, e, alpha)
+
+
+def test_guarded_lane_hamming_full_blocks():
+    """Every position a hit for both lanes (32 per block fill the 6-bit count
+    fields), and a lane whose mismatches all sit in its top bit."""
+    for l in (5, 12):
+        text = "A" * 100
+        assert hclr_counts(["A" * l, "A" * l], text, l, 0) == [hamming_hits("A" * l, text, 0)] * 2
+        p1 = "A" * (l - 1) + "C"
+        assert hclr_counts(["A" * l, p1], text, l, 1) == [hamming_hits("A" * l, text, 1), hamming_hits(p1, text, 1)]
+
+
 # ------------------------------------- structured lanes of different lengths
 
 def struct_shape(l0, e0, b1, e1):

@@ -295,7 +295,7 @@ struct MiniJob
     uint32_t             ctas;           // CTAs of this job (<= the grid's x)
     uint8_t              cmap[256];
 };
-constexpr uint32_t kMiniMaxCtas = 16;
+constexpr uint32_t kMiniMaxCtas = 64;              // CTAs per job: one per 1024 symbols, at most this
 __global__ void k_mini_clear ( const MiniJob * jobs );
 __global__ void k_mini_pack ( const MiniJob * jobs );
 __global__ void k_mini_uniq ( const MiniJob * jobs );

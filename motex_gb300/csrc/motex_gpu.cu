@@ -1772,8 +1772,9 @@ int run_mini ( motex_ctx * c, std::vector<Job *> & js, float * dp_ms )
         m.result = dres + 4 * i;
         m.part = static_cast<uint32_t *> ( c->mpart.p ) + ( size_t ) i * kMiniMaxCtas;
         m.nwords = j->nwords;
-        // a CTA per 4096 symbols, at most kMiniMaxCtas
-        m.ctas = ( uint32_t ) std::min<uint64_t> ( kMiniMaxCtas, std::max<uint64_t> ( 1, ( j->total + 4095 ) / 4096 ) );
+        // the stages around the DP are latency-bound (a few dependent loads and
+        // atomics per position or factor): one 1024-thread CTA per 1024 symbols
+        m.ctas = ( uint32_t ) std::min<uint64_t> ( kMiniMaxCtas, std::max<uint64_t> ( 1, ( j->total + 1023 ) / 1024 ) );
         max_ctas = std::max ( max_ctas, m.ctas );
         memcpy ( m.cmap, pin<uint8_t> ( j, kPinCmap ), 256 );
         pin<uint32_t> ( j, kPinScalar )[2] = 0;                     // no key table and no staging wait

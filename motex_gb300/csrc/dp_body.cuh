@@ -772,7 +772,7 @@ __device__ __forceinline__ void dp_hswar_body ( const DPArgs & a, const SwarCons
         for ( int i = 0; i < W; ++i )
         {
 #pragma unroll
-            for ( int j = 0; j < NL; ++j ) s_cnt[( i * NL + j ) * kDPThreads + tid] += ( cnt[i] >> ( j * C.S + C.Q ) ) & C.FM;
+            for ( int j = 0; j < NL; ++j ) s_cnt[( i * NL + j ) * kDPThreads + tid] += ( cnt[i] >> ( j * C.S + ( E >= 0 ? C.Q : 0u ) ) ) & C.FM;
             cnt[i] = 0;
         }
     };

@@ -204,30 +204,6 @@ __device__ __forceinline__ void bulk_copy_g2s ( void * dst, const void * src, ui
                    : "memory" );
 }
 
-// Low 32 bits of the key of the factor ending at each lane's position (its
-// last `win` symbols, B bits each, the last one lowest): c = this step's
-// codes, pk = the previous step's keys.  Window sizes double per level; a
-// lane below s takes the low s symbols of the previous step's key.  Only the
-// low 32 bits are kept at every level: bits shifted past 32 never come back
-// down, so the truncated doubling gives the truncated key (s * B < 32 on
-// every level that runs, since s < win <= 31 / B + 1).
-__device__ __forceinline__ uint32_t pack_keys ( uint32_t c, uint32_t pk, uint32_t win, uint32_t B, int lane )
-{
-    uint32_t y = c;
-#pragma unroll
-    for ( int lv = 0; lv < 5; ++lv )                 // s = 1, 2, 4, 8, 16 while s < win (warp-uniform)
-    {
-        const uint32_t s = 1u << lv;
-        if ( s >= win ) break;
-        const uint32_t cur = __shfl_up_sync ( 0xffffffffu, y, s );
-        const uint32_t old = __shfl_sync ( 0xffffffffu, pk, ( lane + 32 - ( int ) s ) & 31 );
-        const uint32_t sb = s * B;
-        const uint32_t src = lane >= ( int ) s ? cur : ( old & ( ( 1u << sb ) - 1u ) );
-        y |= src << sb;
-    }
-    return y;
-}
-
 } // namespace
 
 /*
@@ -660,32 +636,77 @@ __global__ void __launch_bounds__ ( kSortThreads ) k_radix_scatter ( const uint3
 // keys[i] is the most significant key chunk of factor idx[i] (sorted order,
 // coalesced); when it is the whole factor (full_key) it decides alone,
 // otherwise equal chunks fall back to comparing the symbols.
+// Four flags per thread: one 16-byte load of their keys (keys and head are
+// allocation bases, 16-byte aligned) and one 4-byte store of the flags.
 __global__ void k_heads ( const uint32_t * __restrict__ idx, const uint32_t * __restrict__ keys, int full_key,
                           uint32_t n, const uint8_t * __restrict__ codes, uint32_t l, uint8_t * __restrict__ head )
 {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if ( i >= n ) return;
-    uint8_t h = 1;
-    if ( i > 0 && keys[i] == keys[i - 1] )
+    const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x, i0 = q * 4;
+    if ( i0 >= n ) return;
+    const bool whole = i0 + 4 <= n;
+    uint32_t k[5];
+    k[0] = i0 > 0 ? keys[i0 - 1] : 0u;
+    if ( whole )
     {
-        h = 0;
-        if ( ! full_key )
-        {
-            const uint32_t p = idx[i], q = idx[i - 1];
-            for ( uint32_t e = 0; e < l; ++e )
-                if ( codes[p - e] != codes[q - e] ) { h = 1; break; }
-        }
+        const uint4 v = reinterpret_cast<const uint4 *> ( keys )[q];
+        k[1] = v.x; k[2] = v.y; k[3] = v.z; k[4] = v.w;
     }
-    head[i] = h;
+    else
+        for ( uint32_t t = 0; t < 4; ++t ) k[t + 1] = i0 + t < n ? keys[i0 + t] : 0u;
+    uint32_t hw = 0;
+#pragma unroll
+    for ( uint32_t t = 0; t < 4; ++t )
+    {
+        const uint32_t i = i0 + t;
+        if ( i >= n ) break;                    // the last group: no flag, no key, no factor past n
+        uint32_t h = 1;
+        if ( i > 0 && k[t + 1] == k[t] )
+        {
+            h = 0;
+            if ( ! full_key )
+            {
+                const uint32_t p = idx[i], pq = idx[i - 1];
+                for ( uint32_t e = 0; e < l; ++e )
+                    if ( codes[p - e] != codes[pq - e] ) { h = 1; break; }
+            }
+        }
+        hw |= h << ( 8 * t );
+    }
+    if ( whole ) reinterpret_cast<uint32_t *> ( head )[q] = hw;
+    else
+        for ( uint32_t t = 0; i0 + t < n; ++t ) head[i0 + t] = ( uint8_t ) ( hw >> ( 8 * t ) );
 }
 
-// Grid-stride (a few CTAs per SM): heads are sparse on repetitive inputs,
-// where one thread per flag made the launch itself the cost.
+// A flag array's 16-byte chunk c as four words (the last, partial chunk from
+// byte loads; flags is 16-byte aligned).
+__device__ __forceinline__ uint4 flag_chunk ( const uint8_t * __restrict__ flags, uint32_t n, uint32_t c )
+{
+    const uint32_t base = c * 16;
+    if ( base + 16 <= n ) return reinterpret_cast<const uint4 *> ( flags )[c];
+    uint32_t w[4] = { 0, 0, 0, 0 };
+    for ( uint32_t k = 0; base + k < n; ++k ) w[k >> 2] |= ( uint32_t ) flags[base + k] << ( 8 * ( k & 3 ) );
+    return make_uint4 ( w[0], w[1], w[2], w[3] );
+}
+
+// Grid-stride (a few CTAs per SM) over 16-flag chunks read as one 16-byte
+// load: heads are sparse on repetitive inputs, where one byte load per
+// thread made the instruction count the cost.
 __global__ void k_unique ( const uint32_t * __restrict__ idx, const uint8_t * __restrict__ head,
                            const uint32_t * __restrict__ pref, uint32_t n, uint32_t * __restrict__ uniq_pos )
 {
-    for ( uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x )
-        if ( head[i] ) uniq_pos[pref[i]] = idx[i];
+    const uint32_t nc = ( n + 15 ) / 16;
+    for ( uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += gridDim.x * blockDim.x )
+    {
+        const uint4 q = flag_chunk ( head, n, c );
+        const uint32_t w[4] = { q.x, q.y, q.z, q.w };
+#pragma unroll
+        for ( int k = 0; k < 16; ++k )
+            if ( ( w[k >> 2] >> ( 8 * ( k & 3 ) ) ) & 255u )
+            {
+                const uint32_t i = c * 16 + k;
+                uniq_pos[pref[i]] = idx[i];
+            }
+    }
 }
 
 /*
@@ -762,18 +783,25 @@ __global__ void k_finalize ( FinalizeArgs a )
     }
 }
 
-// Grid-stride like k_unique (marks are sparse).
+// Grid-stride over 16-mark chunks like k_unique (marks are sparse).
 __global__ void k_compact ( const uint8_t * __restrict__ mark, const uint32_t * __restrict__ pref, uint32_t n,
                             const uint32_t * __restrict__ rec_u, const uint32_t * __restrict__ rec_v,
                             uint32_t * __restrict__ out )
 {
-    for ( uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x )
+    const uint32_t nc = ( n + 15 ) / 16;
+    for ( uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += gridDim.x * blockDim.x )
     {
-        if ( ! mark[p] ) continue;
-        const uint32_t j = pref[p];
-        out[3 * ( size_t ) j + 0] = p;
-        out[3 * ( size_t ) j + 1] = rec_u[p];
-        out[3 * ( size_t ) j + 2] = rec_v[p];
+        const uint4 q = flag_chunk ( mark, n, c );
+        const uint32_t w[4] = { q.x, q.y, q.z, q.w };
+#pragma unroll
+        for ( int k = 0; k < 16; ++k )
+            if ( ( w[k >> 2] >> ( 8 * ( k & 3 ) ) ) & 255u )
+            {
+                const uint32_t p = c * 16 + k, j = pref[p];
+                out[3 * ( size_t ) j + 0] = p;
+                out[3 * ( size_t ) j + 1] = rec_u[p];
+                out[3 * ( size_t ) j + 2] = rec_v[p];
+            }
     }
 }
 

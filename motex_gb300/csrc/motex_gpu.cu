@@ -754,7 +754,7 @@ int stage_pack ( Job * j, bool * need_sync )
         uint32_t * pref;
         MTX_TRY ( ensure ( j, S_HEAD, j->nwords, &head ) );
         MTX_TRY ( ensure ( j, S_PREF, j->nwords, &pref ) );
-        MTX_LAUNCH ( k_heads, blocks_for ( j->nwords, 256 ), 256, idx, keys, ( int ) full_key, j->nwords, codes, P.l, head );
+        MTX_LAUNCH ( k_heads, blocks_for ( ( j->nwords + 3 ) / 4, 256 ), 256, idx, keys, ( int ) full_key, j->nwords, codes, P.l, head );
         MTX_TRY ( scan_flags ( j, head, j->nwords, pref, scalar ) );
         MTX_CUDA ( cudaMemcpyAsync ( pin<uint32_t> ( j, kPinScalar ), scalar, 4, cudaMemcpyDeviceToHost, st ) );
         j->uniq = idx;                               // sorted factor ends; compacted in stage_plan
@@ -786,7 +786,7 @@ int stage_plan ( Job * j, bool sorted )
         if ( ! j->replaying ) j->U = pin<uint32_t> ( j, kPinScalar )[0];
         uint32_t * uniq;
         MTX_TRY ( ensure ( j, S_UNIQ, j->U, &uniq ) );
-        MTX_LAUNCH ( k_unique, std::min<unsigned> ( blocks_for ( j->nwords, 256 ), 8 * j->ctx->num_sms ), 256, j->uniq,
+        MTX_LAUNCH ( k_unique, std::min<unsigned> ( blocks_for ( ( j->nwords + 15 ) / 16, 256 ), 8 * j->ctx->num_sms ), 256, j->uniq,
                      dptr<uint8_t> ( j, S_HEAD ),
                      dptr<uint32_t> ( j, S_PREF ), j->nwords, uniq );
         j->uniq = uniq;
@@ -1228,7 +1228,7 @@ int stage_compact ( Job * j )
         const uint32_t n = ( uint32_t ) ( j->structured ? j->total * j->G : j->total );
         uint32_t * recs;
         MTX_TRY ( ensure ( j, S_RECS, ( size_t ) 3 * std::max<uint32_t> ( 1, j->nrec ), &recs ) );
-        MTX_LAUNCH ( k_compact, std::min<unsigned> ( blocks_for ( n, 256 ), 8 * j->ctx->num_sms ), 256,
+        MTX_LAUNCH ( k_compact, std::min<unsigned> ( blocks_for ( ( n + 15 ) / 16, 256 ), 8 * j->ctx->num_sms ), 256,
                      dptr<uint8_t> ( j, S_MARK ), dptr<uint32_t> ( j, S_PREF2 ), n,
                      dptr<uint32_t> ( j, S_RECU ), dptr<uint32_t> ( j, S_RECV ), recs );
         if ( j->structured && j->nrec )

@@ -110,10 +110,73 @@ static cudaError_t scan_exclusive_impl ( const T * in, uint32_t n, uint32_t * ou
     return cudaGetLastError ();
 }
 
+// Byte flags: a thread owns 16 consecutive bytes, read as one 16-byte load
+// (in is an allocation base), and writes their 16 prefix words as four
+// 16-byte stores; a tile is 16 times the thread count.
+constexpr int kScanItemsU8 = 16;
+constexpr uint32_t kScanTileU8 = kScanThreads * kScanItemsU8;
+
+__device__ __forceinline__ uint4 load16_u8 ( const uint8_t * __restrict__ in, uint32_t n, uint32_t base )
+{
+    if ( base + 16 <= n ) return *reinterpret_cast<const uint4 *> ( in + base );
+    uint32_t w[4] = { 0, 0, 0, 0 };
+    for ( uint32_t k = 0; base + k < n; ++k ) w[k >> 2] |= ( uint32_t ) in[base + k] << ( 8 * ( k & 3 ) );
+    return make_uint4 ( w[0], w[1], w[2], w[3] );
+}
+
+__device__ __forceinline__ uint32_t byte_sum ( const uint4 & q )
+{
+    return __dp4a ( q.x, 0x01010101u, 0u ) + __dp4a ( q.y, 0x01010101u, 0u ) + __dp4a ( q.z, 0x01010101u, 0u ) +
+           __dp4a ( q.w, 0x01010101u, 0u );
+}
+
+__global__ void __launch_bounds__ ( kScanThreads ) k_tile_reduce_u8 ( const uint8_t * __restrict__ in, uint32_t n,
+                                                                      uint32_t * tile_sums )
+{
+    const uint32_t base = blockIdx.x * kScanTileU8 + threadIdx.x * kScanItemsU8;
+    const uint32_t s = base < n ? byte_sum ( load16_u8 ( in, n, base ) ) : 0u;
+    uint32_t tot;
+    block_exclusive_scan ( s, &tot );
+    if ( threadIdx.x == 0 ) tile_sums[blockIdx.x] = tot;
+}
+
+__global__ void __launch_bounds__ ( kScanThreads ) k_tile_scan_u8 ( const uint8_t * __restrict__ in, uint32_t n,
+                                                                    const uint32_t * tile_off, uint32_t * out )
+{
+    const uint32_t base = blockIdx.x * kScanTileU8 + threadIdx.x * kScanItemsU8;
+    const uint4 q = base < n ? load16_u8 ( in, n, base ) : make_uint4 ( 0, 0, 0, 0 );
+    uint32_t run = tile_off[blockIdx.x] + block_exclusive_scan ( byte_sum ( q ), nullptr );
+    const uint32_t w[4] = { q.x, q.y, q.z, q.w };
+    uint32_t o[16];
+#pragma unroll
+    for ( int r = 0; r < 16; ++r )
+    {
+        o[r] = run;
+        run += ( w[r >> 2] >> ( 8 * ( r & 3 ) ) ) & 255u;
+    }
+    if ( base + 16 <= n )
+    {
+        uint4 * dst = reinterpret_cast<uint4 *> ( out + base );
+#pragma unroll
+        for ( int r = 0; r < 4; ++r ) dst[r] = make_uint4 ( o[4 * r], o[4 * r + 1], o[4 * r + 2], o[4 * r + 3] );
+    }
+    else
+    {
+#pragma unroll
+        for ( int r = 0; r < 16; ++r )
+            if ( base + r < n ) out[base + r] = o[r];
+    }
+}
+
+// tile_sums holds at least ceil(n / kScanTileU8) words (ceil(n / kScanTile) is more)
 cudaError_t scan_exclusive_u8 ( const uint8_t * in, uint32_t n, uint32_t * out, uint32_t * d_total,
                                 uint32_t * tile_sums, cudaStream_t st )
 {
-    return scan_exclusive_impl<uint8_t> ( in, n, out, d_total, tile_sums, st );
+    const uint32_t tiles = ( n + kScanTileU8 - 1 ) / kScanTileU8;
+    k_tile_reduce_u8<<<tiles ? tiles : 1, kScanThreads, 0, st>>> ( in, n, tile_sums );
+    k_scan_single<<<1, kScanThreads, 0, st>>> ( tile_sums, tiles ? tiles : 1, d_total );
+    k_tile_scan_u8<<<tiles ? tiles : 1, kScanThreads, 0, st>>> ( in, n, tile_sums, out );
+    return cudaGetLastError ();
 }
 
 cudaError_t scan_exclusive_u32 ( const uint32_t * in, uint32_t n, uint32_t * out, uint32_t * d_total,

@@ -546,9 +546,13 @@ int autotune ( Job * j, DPTune * best )
     }
     if ( ! ed && hclr_eligible ( j->prm.l, j->prm.e ) )
         for ( int W : { 4, 8 } ) cands.push_back ( DPTune { W, hclr_lanes ( j->prm.l ), 4, 1 } );
-    // probe chunks: consecutive 512-block ranges from the start of the text, no splits
+    // probe chunks: consecutive 512-block ranges from the start of the text, no
+    // splits; up to 64, so that a job with few factor tiles (a few thousand
+    // distinct factors) still fills every SM in the probe as in the real grid
+    // (with 16, a 4-tile shape ran 64 CTAs on 152 SMs and lost to a shape with
+    // more tiles that is slower at full occupancy)
     const uint32_t pblk = std::min<uint32_t> ( j->nblk, kTuneBlocks );
-    const uint32_t maxc = std::max<uint32_t> ( 1, std::min<uint32_t> ( 16, j->nblk / pblk ) );
+    const uint32_t maxc = std::max<uint32_t> ( 1, std::min<uint32_t> ( 64, j->nblk / pblk ) );
     ChunkInfo * d_probe;
     MTX_TRY ( ensure ( j, S_TILES, maxc * ( ( sizeof ( ChunkInfo ) + 3 ) / 4 ), reinterpret_cast<uint32_t **> ( &d_probe ) ) );
     ChunkInfo * h_probe = pin<ChunkInfo> ( j, kPinChunks );
@@ -786,7 +790,7 @@ int stage_plan ( Job * j, bool sorted )
         if ( ! j->replaying ) j->U = pin<uint32_t> ( j, kPinScalar )[0];
         uint32_t * uniq;
         MTX_TRY ( ensure ( j, S_UNIQ, j->U, &uniq ) );
-        MTX_LAUNCH ( k_unique, std::min<unsigned> ( blocks_for ( ( j->nwords + 15 ) / 16, 256 ), 8 * j->ctx->num_sms ), 256, j->uniq,
+        MTX_LAUNCH ( k_unique, std::min<unsigned> ( blocks_for ( ( j->nwords + 15 ) / 16, 256 ), 64 * j->ctx->num_sms ), 256, j->uniq,
                      dptr<uint8_t> ( j, S_HEAD ),
                      dptr<uint32_t> ( j, S_PREF ), j->nwords, uniq );
         j->uniq = uniq;
@@ -1228,7 +1232,7 @@ int stage_compact ( Job * j )
         const uint32_t n = ( uint32_t ) ( j->structured ? j->total * j->G : j->total );
         uint32_t * recs;
         MTX_TRY ( ensure ( j, S_RECS, ( size_t ) 3 * std::max<uint32_t> ( 1, j->nrec ), &recs ) );
-        MTX_LAUNCH ( k_compact, std::min<unsigned> ( blocks_for ( ( n + 15 ) / 16, 256 ), 8 * j->ctx->num_sms ), 256,
+        MTX_LAUNCH ( k_compact, std::min<unsigned> ( blocks_for ( ( n + 15 ) / 16, 256 ), 64 * j->ctx->num_sms ), 256,
                      dptr<uint8_t> ( j, S_MARK ), dptr<uint32_t> ( j, S_PREF2 ), n,
                      dptr<uint32_t> ( j, S_RECU ), dptr<uint32_t> ( j, S_RECV ), recs );
         if ( j->structured && j->nrec )

@@ -286,8 +286,8 @@ def dp_kernel_name(wl):
     B = max(2, (sigma - 1).bit_length())
     if wl.d == 1 and 4 <= wl.k <= 15:
         return f"k_dp_swar_ed (NL={min(4, 33 // (wl.k + 1))})"
-    if wl.d == 0 and B <= 3 and 5 <= wl.k <= 12 and wl.e <= 3:
-        return "k_dp_hclr (NL=2)"
+    if wl.d == 0 and 5 <= wl.k <= 12 and wl.e <= 3:
+        return f"k_dp_hclr (NL={3 if 6 <= wl.k <= 10 else 2})"
     if wl.d == 0 and B >= 3 and 6 <= wl.k <= 16:
         return f"k_dp_hswar (NL={32 // wl.k})"
     return "k_dp_fast"

@@ -701,6 +701,12 @@ __device__ __forceinline__ void dp_swar_body ( const DPArgs & a, const SwarConst
  * the count add are multiply-adds (FMA pipe); no popc.  C holds S = l+1,
  * HB = the guard bits G, K = -L, REP = sum 2^(j*S), Q = l (count field
  * offset in a lane) and FM = 63.
+ *
+ * NL = 3 (6 <= l <= 10): the top lane, at 2S, has no guard (for l = 10 it
+ * ends at bit 31).  Its clears need none: a borrow out of it leaves the
+ * register or lands in bits that x and the AND keep zero.  It is zero
+ * exactly when x < LIM = 2^(2S), and that hit is counted by one compare and
+ * add into a count field at bit 0 (below lane 0's count field at bit l).
  */
 template <int B, int NL, int W, int UR, int E = -1>
 __device__ __forceinline__ void dp_hswar_body ( const DPArgs & a, const SwarConst & C, uint32_t tile, uint32_t chunk )
@@ -750,6 +756,8 @@ __device__ __forceinline__ void dp_hswar_body ( const DPArgs & a, const SwarCons
 #pragma unroll
             for ( int c = 0; c < E; ++c ) x = ( x & ( x * C.ONE + C.K ) ) | C.HB;
             cnt[i] = ( ~( x * C.ONE + C.K ) & C.HB ) * C.ONE + cnt[i];
+            if constexpr ( NL == 3 )
+                if ( x < C.LIM ) cnt[i] += 1u;
         }
         else
         {
@@ -772,7 +780,7 @@ __device__ __forceinline__ void dp_hswar_body ( const DPArgs & a, const SwarCons
         for ( int i = 0; i < W; ++i )
         {
 #pragma unroll
-            for ( int j = 0; j < NL; ++j ) s_cnt[( i * NL + j ) * kDPThreads + tid] += ( cnt[i] >> ( j * C.S + ( E >= 0 ? C.Q : 0u ) ) ) & C.FM;
+            for ( int j = 0; j < NL; ++j ) s_cnt[( i * NL + j ) * kDPThreads + tid] += ( cnt[i] >> ( E < 0 ? j * C.S : ( NL == 3 && j == 2 ? 0u : j * C.S + C.Q ) ) ) & C.FM;
             cnt[i] = 0;
         }
     };

@@ -233,6 +233,7 @@ struct SwarConst
     // of 6 bits at h); NL = 4 (too narrow for that): h = l-1, and the count
     // shifts the hit bits to the lane base
     uint32_t HQ, Q;
+    uint32_t LIM;    // guarded-lane Hamming with three lanes: 2^(2S), the top lane's base
     uint32_t REP;    // Hamming lanes: sum of 2^(j*l), replicates an l-bit window into every lane
     // Multipliers of the edit-distance step, kernel parameters so that the
     // compiler cannot fold them: x * ONE + y, x * TWO and x * NEG1 + y run as
@@ -248,11 +249,14 @@ int hswar_lanes ( uint32_t l );
 SwarConst hswar_const ( uint32_t l, int NL );
 bool launch_dp_hswar ( const DPArgs & a, int B, int NL, int W, int UR, dim3 grid, cudaStream_t st );
 // Popc-free Hamming for e <= kHclrMaxE: two factors of l bits per register in
-// guarded lanes (5 <= l <= 12), mismatches counted by clearing each lane's
-// lowest set bit e times (dp_hclr.cu); unroll 4.
+// guarded lanes (5 <= l <= 12), or three (6 <= l <= 10, the top lane tested
+// by a compare), mismatches counted by clearing each lane's lowest set bit e
+// times (dp_hclr.cu); unroll 4.  hclr_lanes: the default lane count for l
+// (3 where it fits), hclr_fits: whether NL lanes fit l.
 constexpr uint32_t kHclrMaxE = 3;
 int hclr_lanes ( uint32_t l );
-SwarConst hclr_const ( uint32_t l );
+bool hclr_fits ( uint32_t l, int NL );
+SwarConst hclr_const ( uint32_t l, int NL );
 bool launch_dp_hclr ( const DPArgs & a, int B, int NL, int W, dim3 grid, cudaStream_t st );
 // Register words per thread of the packed kernels when the shape is not tuned
 // (batched jobs, persistent launches, the default of an untuned job): with

@@ -388,21 +388,23 @@ int sort_factors ( Job * j, uint32_t n, uint32_t ** idx_out, const uint32_t ** k
  * 32-position text block (UR, bounded to keep the loop in the instruction
  * cache).  MOTEX_DP_W / MOTEX_DP_UR / MOTEX_DP_SWAR=0 override the choice.
  */
-bool hclr_eligible ( uint32_t l, uint32_t e ) { return e <= kHclrMaxE && hclr_lanes ( l ) == 2; }
+bool hclr_eligible ( uint32_t l, uint32_t e ) { return e <= kHclrMaxE && hclr_lanes ( l ) >= 2; }
 
 DPTune choose_tune ( Job * j, uint32_t U, bool ed, bool generic )
 {
     DPTune t;
     if ( generic ) { t.W = 1; t.NL = 1; t.UR = 32; return t; }
     t.NL = ed ? swar_lanes ( j->prm.l ) : ( j->B >= 3 ? hswar_lanes ( j->prm.l ) : 1 );
-    // Hamming with e <= 3 and 5 <= l <= 12 over 2-3 bit planes: the popc-free
-    // guarded-lane form by default (measured on GB300: config 1 DP 0.235 ->
-    // 0.201 ms; with 4-5 planes the three-lane popc form stays ahead, the
-    // autotuner tries both); MOTEX_DP_CLEAR=0 keeps the popc forms
+    // Hamming with e <= 3 and 5 <= l <= 12: the popc-free guarded-lane form,
+    // three lanes where they fit (measured on GB300: config 1 DP 0.235 ->
+    // 0.201 ms with two lanes; config 3 Hamming 268 -> 207 ms with three).
+    // MOTEX_DP_CLEAR: 0 keeps the popc forms; 2 or 3 fixes the lane count
+    // where that fits
     const char * clr = getenv ( "MOTEX_DP_CLEAR" );
-    if ( ! ed && j->B <= 3 && hclr_eligible ( j->prm.l, j->prm.e ) && ! ( clr && atoi ( clr ) == 0 ) )
+    const int clr_v = clr ? atoi ( clr ) : -1;
+    if ( ! ed && hclr_eligible ( j->prm.l, j->prm.e ) && clr_v != 0 )
     {
-        t.NL = hclr_lanes ( j->prm.l );
+        t.NL = ( clr_v >= 2 && hclr_fits ( j->prm.l, clr_v ) ) ? clr_v : hclr_lanes ( j->prm.l );
         t.F = 1;
     }
     const uint32_t groups = ( U + t.NL - 1 ) / t.NL;
@@ -464,7 +466,7 @@ bool tune_entry_valid ( const TuneKey & k, const DPTune & t )
     if ( k.B < 2 || k.B > kMaxPlanes || k.l < 1 || k.l > 32 || k.e >= k.l || k.d > 1 ) return false;
     if ( t.W != 4 && t.W != 8 ) return false;
     if ( t.F != 0 )                                         // guarded-lane Hamming
-        return t.F == 1 && k.d == 0 && hclr_eligible ( k.l, k.e ) && t.NL == hclr_lanes ( k.l ) && t.UR == 4;
+        return t.F == 1 && k.d == 0 && k.e <= kHclrMaxE && hclr_fits ( k.l, t.NL ) && t.UR == 4;
     const int packed = k.d == 1 ? swar_lanes ( k.l ) : ( k.B >= 3 ? hswar_lanes ( k.l ) : 1 );
     if ( t.NL != 1 && ( t.NL != packed || packed < 2 ) ) return false;
     if ( t.UR != 4 && t.UR != 8 && ! ( t.UR == 32 && t.NL == 1 ) ) return false;
@@ -545,7 +547,9 @@ int autotune ( Job * j, DPTune * best )
         if ( NL == 1 ) break;
     }
     if ( ! ed && hclr_eligible ( j->prm.l, j->prm.e ) )
-        for ( int W : { 4, 8 } ) cands.push_back ( DPTune { W, hclr_lanes ( j->prm.l ), 4, 1 } );
+        for ( int NL : { 3, 2 } )
+            if ( hclr_fits ( j->prm.l, NL ) )
+                for ( int W : { 4, 8 } ) cands.push_back ( DPTune { W, NL, 4, 1 } );
     // probe chunks: consecutive 512-block ranges from the start of the text, no
     // splits; up to 64, so that a job with few factor tiles (a few thousand
     // distinct factors) still fills every SM in the probe as in the real grid

@@ -1,9 +1,11 @@
-"""The popc-free Hamming form (k_dp_hclr: two factors per register in
-guarded lanes, mismatches counted by clearing each lane's lowest set bit e
-times), the default for Hamming with e <= 3 and 5 <= l <= 12: motexGPU
-against the oracle CLI on seeded inputs with planted approximate
-occurrences, with W = 4 and W = 8 register words per thread, and against
-the popc forms (MOTEX_DP_CLEAR=0) on the same input."""
+"""The popc-free Hamming form (k_dp_hclr: two or three factors per register
+in guarded lanes, the third unguarded and tested by a compare, mismatches
+counted by clearing each lane's lowest set bit e times), the default for
+Hamming with e <= 3 and 5 <= l <= 12: motexGPU against
+the oracle CLI on seeded inputs with planted approximate occurrences, for
+DNA and protein, with two and three lanes (MOTEX_DP_CLEAR=2 / 3) and W = 4
+and W = 8 register words per thread, and the popc forms (MOTEX_DP_CLEAR=0)
+on the same input."""
 import random
 
 import pytest
@@ -43,11 +45,14 @@ def test_guarded_lanes_vs_oracle(native_built, oracle_port, monkeypatch, l, e, k
     args = ["-a", kind, "-i", "in.fa", "-o", "out.motex", "-d", "0", "-k", str(l), "-e", str(e), "-q", "20"]
     o = run_cli(oracle_port, None, args + ["-t", "8"], files=files)
     assert o[0] == 0, o[2]
-    for w in ("4", "8"):
-        monkeypatch.setenv("MOTEX_DP_W", w)
-        g = run_cli(native_built.CLI_PATH, None, args, files=files)
-        assert g[0] == 0, g[2]
-        assert g[1] == o[1], (w, l, e, kind)
+    lanes = [nl for nl in (2, 3) if (nl == 2 and 5 <= l <= 12) or (nl == 3 and 6 <= l <= 10)]
+    for nl in lanes:
+        monkeypatch.setenv("MOTEX_DP_CLEAR", str(nl))
+        for w in ("4", "8"):
+            monkeypatch.setenv("MOTEX_DP_W", w)
+            g = run_cli(native_built.CLI_PATH, None, args, files=files)
+            assert g[0] == 0, g[2]
+            assert g[1] == o[1], (nl, w, l, e, kind)
     monkeypatch.delenv("MOTEX_DP_W")
     monkeypatch.setenv("MOTEX_DP_CLEAR", "0")
     p = run_cli(native_built.CLI_PATH, None, args, files=files)

@@ -224,16 +224,18 @@ def test_packed_hamming_needs_six_bit_lanes():
 # ------------------------------- popc-free Hamming: guarded lanes, bit clears
 
 def hclr_counts(pats, text, l, e):
-    """dp_hswar_body with E = e (hclr_const in dp_hclr.cu) restated: two
-    factors of l bits in lanes at 0 and S = l+1 with a guard bit above each,
-    set in the mismatch word; e times x = (x & (x - L)) | G clears each lane's
-    lowest set bit; the hits are ~(x - L) & G (a lane that is zero borrows
-    its guard), added into 6-bit count fields at the guards and drained every
-    32 positions."""
+    """dp_hswar_body with E = e (hclr_const in dp_hclr.cu) restated: two or
+    three factors of l bits in lanes at 0, S = l+1 (and 2S) with a guard bit
+    above each lane but the third, set in the mismatch word; e times
+    x = (x & (x - L)) | G clears each lane's lowest set bit; the hits of the
+    guarded lanes are ~(x - L) & G (a lane that is zero borrows its guard),
+    added into 6-bit count fields at the guards; the third lane's hit is
+    x < 2^(2S), counted at bit 0; drained every 32 positions."""
     NL, S = len(pats), l + 1
-    assert NL == 2 and 5 <= l <= 12 and e <= 3
-    G = sum(1 << (j * S + l) for j in range(NL))
+    assert (NL == 2 and 5 <= l <= 12 or NL == 3 and 6 <= l <= 10) and e <= 3
+    G = sum(1 << (j * S + l) for j in range(2))
     L = sum(1 << (j * S) for j in range(NL))
+    LIM = 1 << (2 * S)
     codes = {c: i for i, c in enumerate(sorted(set(text) | set("".join(pats))))}
     nbits = max(1, (len(codes) - 1).bit_length())
     fp = [0] * nbits
@@ -254,20 +256,22 @@ def hclr_counts(pats, text, l, e):
             for _ in range(e):
                 x = ((x & ((x - L) & M32)) | G) & M32
             cnt = (cnt + (~((x - L) & M32) & G)) & M32
+            if NL == 3 and x < LIM:
+                cnt += 1
         if k % 32 == 31 or k == len(text) - 1:
             for j in range(NL):
-                counts[j] += (cnt >> (j * S + l)) & 63
+                counts[j] += (cnt >> (0 if j == 2 else j * S + l)) & 63
             cnt = 0
     return counts
 
 
-@pytest.mark.parametrize("l", range(5, 13))
-def test_guarded_lane_hamming_matches(l):
-    rng = random.Random(500 + l)
+@pytest.mark.parametrize("l,NL", [(l, 2) for l in range(5, 13)] + [(l, 3) for l in range(6, 11)])
+def test_guarded_lane_hamming_matches(l, NL):
+    rng = random.Random(500 + 20 * NL + l)
     for e in range(0, min(3, l - 1) + 1):
         for alpha in ("ACGT", "ACDEFGHIKLMNPQRSTVWY"):
             for _ in range(3):
-                pats = ["".join(rng.choice(alpha) for _ in range(l)) for _ in range(2)]
+                pats = ["".join(rng.choice(alpha) for _ in range(l)) for _ in range(NL)]
                 text = "".join(rng.choice(alpha) for _ in range(150))
                 # plant both factors with up to e substitutions
                 for p in pats:
@@ -282,11 +286,12 @@ def test_guarded_lane_hamming_matches(l):
 def test_guarded_lane_hamming_full_blocks():
     """Every position a hit for both lanes (32 per block fill the 6-bit count
     fields), and a lane whose mismatches all sit in its top bit."""
-    for l in (5, 12):
+    for l, NL in ((5, 2), (12, 2), (6, 3), (10, 3)):
         text = "A" * 100
-        assert hclr_counts(["A" * l, "A" * l], text, l, 0) == [hamming_hits("A" * l, text, 0)] * 2
+        assert hclr_counts(["A" * l] * NL, text, l, 0) == [hamming_hits("A" * l, text, 0)] * NL
         p1 = "A" * (l - 1) + "C"
-        assert hclr_counts(["A" * l, p1], text, l, 1) == [hamming_hits("A" * l, text, 1), hamming_hits(p1, text, 1)]
+        pats = ["A" * l] * (NL - 1) + [p1]
+        assert hclr_counts(pats, text, l, 1) == [hamming_hits(p, text, 1) for p in pats]
 
 
 # ------------------------------------- structured lanes of different lengths

@@ -35,7 +35,9 @@ CACHE_LINES = [
     "2 10 4 0 8 2 4 1",    # guarded lanes need e <= 3: rejected
     "2 11 2 0 8 2 8 1",    # guarded lanes with unroll 8: rejected
     "2 11 2 1 8 2 4 1",    # guarded lanes for edit distance: rejected
-    "2 11 3 0 8 3 4 1",    # guarded lanes hold 2 factors: rejected
+    "2 11 3 0 8 3 4 1",    # three guarded lanes need l <= 10: rejected
+    "2 8 2 0 8 3 4 1",     # DNA Hamming, k 8, e 2: three guarded lanes, valid
+    "2 5 1 0 8 3 4 1",     # three guarded lanes need l >= 6: rejected
     "2 11 1 0 8 2 4 2",    # form 2: rejected
     "garbage line",
     "2 18 2 1 4 1 8",      # valid, after the bad lines
@@ -46,12 +48,12 @@ QUERIES = [(2, 15, 3, 1), (5, 10, 2, 1), (5, 10, 2, 0), (2, 20, 3, 0), (2, 12, 2
            (2, 14, 2, 0), (5, 11, 2, 0), (5, 12, 2, 0), (2, 9, 1, 1), (2, 40, 3, 0), (2, 8, 8, 1),
            (7, 8, 1, 1), (2, 16, 2, 1), (2, 17, 2, 1), (2, 18, 2, 1), (2, 15, 3, 0), (3, 15, 3, 1),
            (2, 9, 2, 0), (5, 10, 1, 0), (2, 13, 1, 0), (2, 10, 4, 0), (2, 11, 2, 0), (2, 11, 2, 1),
-           (2, 11, 3, 0), (2, 11, 1, 0)]
+           (2, 11, 3, 0), (2, 11, 1, 0), (2, 8, 2, 0), (2, 5, 1, 0)]
 
 EXPECTED = {(2, 15, 3, 1): [8, 2, 8], (5, 10, 2, 1): [4, 3, 4], (5, 10, 2, 0): [8, 3, 4],
             (2, 20, 3, 0): [8, 1, 32], (2, 18, 2, 1): [8, 1, 4],
             # a negative NL reports the guarded-lane form
-            (2, 9, 2, 0): [8, -2, 4], (5, 10, 1, 0): [4, -2, 4]}
+            (2, 9, 2, 0): [8, -2, 4], (5, 10, 1, 0): [4, -2, 4], (2, 8, 2, 0): [8, -3, 4]}
 
 
 def test_tune_cache_keys_and_validation(native_built, tmp_path):

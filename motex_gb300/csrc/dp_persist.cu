@@ -55,6 +55,22 @@ __global__ void __launch_bounds__ ( kDPThreads ) k_dp_hswar_persist ( const JobD
     }
 }
 
+// popc-free Hamming (guarded lanes, E = e lowest-bit clears), 8 register
+// words per thread, unroll 4
+template <int B, int NL, int E>
+__global__ void __launch_bounds__ ( kDPThreads ) k_dp_hclr_persist ( const JobDesc * jobs, const WorkItem * items,
+                                                                     uint32_t nitems, uint32_t * counter,
+                                                                     const SwarConst C )
+{
+    __shared__ DPArgs s_job;
+    WorkItem w;
+    while ( next_item ( items, nitems, counter, w ) )
+    {
+        load_job ( jobs, w.job, s_job );
+        dp_hswar_body<B, NL, 8, 4, E> ( s_job, C, w.tile, w.chunk );
+    }
+}
+
 template <int B, int NL, int W, int UR>
 __global__ void __launch_bounds__ ( kDPThreads ) k_dp_swar_persist ( const JobDesc * jobs, const WorkItem * items,
                                                                      uint32_t nitems, uint32_t * counter,
@@ -81,10 +97,42 @@ int ctas_per_sm ( K kernel, size_t smem )
     return n > 0 ? n : 1;
 }
 
+template <int B, int NL, int E>
+bool launch_hclr ( const JobDesc * jobs, const WorkItem * items, uint32_t nitems, uint32_t * counter,
+                   const SwarConst & C, unsigned grid, cudaStream_t st, int * occ )
+{
+    const size_t smem = hswar_smem_bytes ( NL, 8 );
+    if ( occ ) { *occ = ctas_per_sm ( k_dp_hclr_persist<B, NL, E>, smem ); return true; }
+    cudaFuncSetAttribute ( k_dp_hclr_persist<B, NL, E>, cudaFuncAttributeMaxDynamicSharedMemorySize, ( int ) smem );
+    k_dp_hclr_persist<B, NL, E><<<grid, kDPThreads, smem, st>>> ( jobs, items, nitems, counter, C );
+    return true;
+}
+
+template <int B, int NL>
+bool launch_hclr_e ( const JobDesc * jobs, const WorkItem * items, uint32_t nitems, uint32_t * counter, int E,
+                     const SwarConst & C, unsigned grid, cudaStream_t st, int * occ )
+{
+    switch ( E )
+    {
+        case 0: return launch_hclr<B, NL, 0> ( jobs, items, nitems, counter, C, grid, st, occ );
+        case 1: return launch_hclr<B, NL, 1> ( jobs, items, nitems, counter, C, grid, st, occ );
+        case 2: return launch_hclr<B, NL, 2> ( jobs, items, nitems, counter, C, grid, st, occ );
+        case 3: return launch_hclr<B, NL, 3> ( jobs, items, nitems, counter, C, grid, st, occ );
+        default: return false;
+    }
+}
+
 template <int B>
 bool launch_b ( const JobDesc * jobs, const WorkItem * items, uint32_t nitems, uint32_t * counter, bool ed, bool scaled,
-                int NL, int W, int UR, const SwarConst & C, unsigned grid, cudaStream_t st, int * occ )
+                int NL, int W, int UR, int E, const SwarConst & C, unsigned grid, cudaStream_t st, int * occ )
 {
+    if ( E >= 0 )
+    {
+        if ( ed || W != 8 || UR != 4 ) return false;
+        if ( NL == 2 ) return launch_hclr_e<B, 2> ( jobs, items, nitems, counter, E, C, grid, st, occ );
+        if ( NL == 3 ) return launch_hclr_e<B, 3> ( jobs, items, nitems, counter, E, C, grid, st, occ );
+        return false;
+    }
     if ( NL <= 1 )
     {
         if ( ! ed )
@@ -162,41 +210,43 @@ bool launch_b ( const JobDesc * jobs, const WorkItem * items, uint32_t nitems, u
 }
 
 bool dispatch ( const JobDesc * jobs, const WorkItem * items, uint32_t nitems, uint32_t * counter, int B, bool ed,
-                bool scaled, int NL, int W, int UR, const SwarConst & C, unsigned grid, cudaStream_t st, int * occ )
+                bool scaled, int NL, int W, int UR, int E, const SwarConst & C, unsigned grid, cudaStream_t st,
+                int * occ )
 {
     switch ( B )
     {
         case 1:
-        case 2: return launch_b<2> ( jobs, items, nitems, counter, ed, scaled, NL, W, UR, C, grid, st, occ );
-        case 3: return launch_b<3> ( jobs, items, nitems, counter, ed, scaled, NL, W, UR, C, grid, st, occ );
-        case 4: return launch_b<4> ( jobs, items, nitems, counter, ed, scaled, NL, W, UR, C, grid, st, occ );
-        case 5: return launch_b<5> ( jobs, items, nitems, counter, ed, scaled, NL, W, UR, C, grid, st, occ );
+        case 2: return launch_b<2> ( jobs, items, nitems, counter, ed, scaled, NL, W, UR, E, C, grid, st, occ );
+        case 3: return launch_b<3> ( jobs, items, nitems, counter, ed, scaled, NL, W, UR, E, C, grid, st, occ );
+        case 4: return launch_b<4> ( jobs, items, nitems, counter, ed, scaled, NL, W, UR, E, C, grid, st, occ );
+        case 5: return launch_b<5> ( jobs, items, nitems, counter, ed, scaled, NL, W, UR, E, C, grid, st, occ );
         default: return false;
     }
 }
 
 } // namespace
 
-int persistent_ctas_per_sm ( int B, bool ed, bool scaled, int NL, int W, int UR )
+int persistent_ctas_per_sm ( int B, bool ed, bool scaled, int NL, int W, int UR, int E )
 {
     int occ = 1;
-    if ( ! dispatch ( nullptr, nullptr, 0, nullptr, B, ed, scaled, NL, W, UR, SwarConst {}, 0, nullptr, &occ ) )
+    if ( ! dispatch ( nullptr, nullptr, 0, nullptr, B, ed, scaled, NL, W, UR, E, SwarConst {}, 0, nullptr, &occ ) )
         return 1;
     return occ;
 }
 
-bool persistent_shape ( int B, bool ed, int NL, int W, int UR )
+bool persistent_shape ( int B, bool ed, int NL, int W, int UR, int E )
 {
+    if ( E >= 0 ) return ! ed && ( NL == 2 || NL == 3 ) && W == 8 && UR == 4 && E <= ( int ) kHclrMaxE;
     if ( NL <= 1 ) return W == 8 && UR == ( ed ? 8 : 4 );
     if ( ! ed ) return B >= 3 && W == 8 && UR == 4;
     return ( W == 4 || W == 8 ) && ( UR == 4 || UR == 8 );
 }
 
 bool launch_dp_persistent ( const JobDesc * jobs, const WorkItem * items, uint32_t nitems, uint32_t * counter, int B,
-                            bool ed, bool scaled, int NL, int W, int UR, const SwarConst & C, unsigned grid,
+                            bool ed, bool scaled, int NL, int W, int UR, int E, const SwarConst & C, unsigned grid,
                             cudaStream_t st )
 {
-    return dispatch ( jobs, items, nitems, counter, B, ed, scaled, NL, W, UR, C, grid, st, nullptr );
+    return dispatch ( jobs, items, nitems, counter, B, ed, scaled, NL, W, UR, E, C, grid, st, nullptr );
 }
 
 } // namespace mtx

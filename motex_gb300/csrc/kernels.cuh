@@ -324,12 +324,14 @@ struct WorkItem
 // the launch has the lane constants C).  grid = resident CTA slots.
 // W register words per thread and block unroll UR: persistent_shape says
 // which the persistent kernels implement (every autotuner choice for packed
-// edit distance; W = 8 with the default unroll otherwise).
+// edit distance; W = 8 with the default unroll otherwise).  E >= 0: the
+// popc-free Hamming form with e = E (NL 2 or 3 guarded lanes, W 8, unroll 4);
+// E = -1 every other form.
 bool launch_dp_persistent ( const JobDesc * jobs, const WorkItem * items, uint32_t nitems, uint32_t * counter,
-                            int B, bool ed, bool scaled, int NL, int W, int UR, const SwarConst & C, unsigned grid,
-                            cudaStream_t st );
-int persistent_ctas_per_sm ( int B, bool ed, bool scaled, int NL, int W, int UR );
-bool persistent_shape ( int B, bool ed, int NL, int W, int UR );
+                            int B, bool ed, bool scaled, int NL, int W, int UR, int E, const SwarConst & C,
+                            unsigned grid, cudaStream_t st );
+int persistent_ctas_per_sm ( int B, bool ed, bool scaled, int NL, int W, int UR, int E );
+bool persistent_shape ( int B, bool ed, int NL, int W, int UR, int E );
 
 // Edit distance, NL = swar_lanes(l) >= 2 factors per 32-bit register (l <= 15);
 // dynamic shared memory swar_smem_bytes ( B, NL, W ).

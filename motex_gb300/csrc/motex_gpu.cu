@@ -1536,9 +1536,11 @@ int batch_dp ( motex_ctx * c, std::vector<Job *> & jobs, float * dp_ms )
         int NL;
         uint32_t l, e;
         int W, UR;
+        int E;                                       // popc-free Hamming: e; otherwise -1
         bool operator< ( const Class & o ) const
         {
-            return std::tie ( B, ed, scaled, NL, l, e, W, UR ) < std::tie ( o.B, o.ed, o.scaled, o.NL, o.l, o.e, o.W, o.UR );
+            return std::tie ( B, ed, scaled, NL, l, e, W, UR, E ) <
+                   std::tie ( o.B, o.ed, o.scaled, o.NL, o.l, o.e, o.W, o.UR, o.E );
         }
     };
     std::map<Class, std::vector<Job *>> classes;
@@ -1560,21 +1562,19 @@ int batch_dp ( motex_ctx * c, std::vector<Job *> & jobs, float * dp_ms )
         DPTune t;
         const bool tuned = ! getenv ( "MOTEX_DP_W" ) && ! getenv ( "MOTEX_DP_UR" ) && ! getenv ( "MOTEX_DP_SWAR" ) &&
                            tune_lookup ( TuneKey { j->B, j->prm.l, j->prm.e, j->prm.d }, &t ) &&
-                           t.F == 0 && persistent_shape ( Bc, ed, t.NL, t.W, t.UR );
+                           persistent_shape ( Bc, ed, t.NL, t.W, t.UR, t.F ? ( int ) j->prm.e : -1 );
         if ( tuned ) j->tune = t;
         else
         {
-            if ( j->tune.F )                        // no persistent guarded-lane kernel: the popc forms
-            {
-                j->tune.F = 0;
-                j->tune.NL = j->B >= 3 ? hswar_lanes ( j->prm.l ) : 1;
-            }
+            // defaults (choose_tune's form and lane count): W = 8 except packed
+            // edit distance, the kernel's unroll
             j->tune.W = ( j->tune.NL > 1 && ed ) ? swar_default_w ( Bc ) : 8;
             j->tune.UR = ( j->tune.NL > 1 ? ( ed ? 8 : 4 ) : ( ed ? 8 : 4 ) );
         }
         const bool packed = j->tune.NL > 1;
+        const int E = j->tune.F ? ( int ) j->prm.e : -1;
         Class k { Bc, ed, ed && j->prm.l <= 28 && j->tune.NL == 1, j->tune.NL,
-                  packed ? j->prm.l : 0u, packed && ed ? j->prm.e : 0u, j->tune.W, j->tune.UR };
+                  packed ? j->prm.l : 0u, packed && ( ed || E >= 0 ) ? j->prm.e : 0u, j->tune.W, j->tune.UR, E };
         const uint32_t groups = ( j->U + j->tune.NL - 1 ) / j->tune.NL;
         j->ntiles = ( groups + kDPThreads * j->tune.W - 1 ) / ( kDPThreads * j->tune.W );
         classes[k].push_back ( j );
@@ -1622,6 +1622,7 @@ int batch_dp ( motex_ctx * c, std::vector<Job *> & jobs, float * dp_ms )
             {
                 hj[jat].a = j->da;
                 hj[jat].C = j->tune.NL <= 1 ? SwarConst {}
+                            : j->tune.F     ? hclr_const ( j->prm.l, j->tune.NL )
                             : ( j->prm.d == 1 ? swar_const ( j->prm.l, j->prm.e, j->tune.NL )
                                               : hswar_const ( j->prm.l, j->tune.NL ) );
                 const uint64_t words = ( uint64_t ) kDPThreads * j->tune.W * j->tune.NL;
@@ -1642,10 +1643,10 @@ int batch_dp ( motex_ctx * c, std::vector<Job *> & jobs, float * dp_ms )
                                          cudaMemcpyHostToDevice, c->st ) );
             MTX_CUDA ( cudaMemcpyAsync ( di + ifirst, hi + ifirst, cn * sizeof ( WorkItem ), cudaMemcpyHostToDevice, c->st ) );
             const Class & k = kv.first;
-            const int per_sm = persistent_ctas_per_sm ( k.B, k.ed, k.scaled, k.NL, k.W, k.UR );
+            const int per_sm = persistent_ctas_per_sm ( k.B, k.ed, k.scaled, k.NL, k.W, k.UR, k.E );
             const unsigned grid = ( unsigned ) std::min<size_t> ( cn, ( size_t ) per_sm * c->num_sms );
             if ( ! launch_dp_persistent ( dj + jfirst, di + ifirst, ( uint32_t ) cn, dcount + ci, k.B, k.ed, k.scaled,
-                                          k.NL, k.W, k.UR, hj[jfirst].C, grid, c->st ) )
+                                          k.NL, k.W, k.UR, k.E, hj[jfirst].C, grid, c->st ) )
                 return fail ( MOTEX_EUNSUPPORTED, "no persistent DP kernel for this class" );
             c->launches++;
             cudaError_t e = cudaGetLastError ();

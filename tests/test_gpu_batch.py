@@ -33,6 +33,25 @@ def test_batch_equals_alone(native_built, gpu_ctx):
 
 
 @pytest.mark.gpu
+def test_batch_guarded_lane_hamming_classes(native_built, gpu_ctx):
+    """Several Hamming jobs of one kernel class run one persistent launch of
+    the popc-free form (two lanes for DNA k 12, three for protein k 10 and
+    k 8); each must equal the same job run alone."""
+    jobs = []
+    for s in range(4):
+        wl = W.dna_hd_small(seed=60 + s, scale=0.1)
+        jobs.append((wl.seqs, native_built.make_params(0, 12, 2, 10)))
+    for s in range(3):
+        wl = W.prot_uneven(seed=70 + s, scale=0.01, d=0)
+        jobs.append((wl.seqs, native_built.make_params(0, 10, 2, 10)))
+        jobs.append((wl.seqs, native_built.make_params(0, 8, 1, 20)))
+    alone = [gpu_ctx.run(seqs, prm).motifs for seqs, prm in jobs]
+    batch = gpu_ctx.run_batch(jobs)
+    assert [b.motifs for b in batch] == alone
+    assert sum(len(m) for m in alone) > 10
+
+
+@pytest.mark.gpu
 def test_repeated_execute_replays_identically(native_built, gpu_ctx):
     wl = W.prot_uneven(seed=49, scale=0.02, d=1)
     prm = native_built.make_params(wl.d, wl.k, wl.e, wl.q)

@@ -313,8 +313,10 @@ def struct_shape(l0, e0, b1, e1):
     return offs, s
 
 
-def struct_hits(words, text, offs, s, es, check=True):
-    """Per lane, per text position: the top-bit hit test of the packed step."""
+def struct_hits(words, text, offs, s, es, check=True, one_shift=False):
+    """Per lane, per text position: the top-bit hit test of the packed step.
+    one_shift: the score update of the kernels whose top lane ends below bit
+    31 (ph - mh as a signed word, one arithmetic shift)."""
     Ls = [len(w) for w in words]
     HB = guards = K = SC0 = 0
     for L, e, o in zip(Ls, es, offs):
@@ -345,7 +347,10 @@ def struct_hits(words, text, offs, s, es, check=True):
         Mhs = Pv & Xh & NGm1
         mh = Pv & Xh & HB
         ph = Ph & HB
-        sc = (sc + (ph >> s) - (mh >> s)) & M32
+        if one_shift:
+            sc = (sc + (signed32((ph - mh) & M32) >> s)) & M32
+        else:
+            sc = (sc + (ph >> s) - (mh >> s)) & M32
         Ph2, Mh2 = (Ph << 1) & M32, (Mhs << 1) & M32
         Pv = (Mh2 | ~(Xv | Ph2)) & M32
         Mv = Ph2 & Xv & NG
@@ -369,6 +374,30 @@ def test_structured_lanes_match_sellers():
         words = ["".join(rng.choice(alpha) for _ in range(L)) for L in (l0, b1, b1)]
         text = "".join(rng.choice(alpha) for _ in range(80))
         got = struct_hits(words, text, offs, s, (e0, e1, e1))
+        for w, e, g in zip(words, (e0, e1, e1), got):
+            assert g == sellers_hits(w, text, e), (l0, e0, b1, e1)
+        done += 1
+
+
+def test_structured_one_shift_update_matches_sellers():
+    """The one-gap and any-gap block kernels take the one-shift score update
+    when the top lane ends below bit 31 (sd in hswar_shape / the any-gap
+    shape): same hits as the two shifts."""
+    rng = random.Random(23)
+    done = 0
+    while done < 300:
+        l0, b1 = rng.randint(2, 14), rng.randint(2, 14)
+        e0, e1 = rng.randint(0, l0 - 1), rng.randint(0, b1 - 1)
+        shape = struct_shape(l0, e0, b1, e1)
+        if shape is None:
+            continue
+        offs, s = shape
+        if offs[2] + b1 - 1 > 30:                   # top lane at bit 31: two shifts
+            continue
+        alpha = rng.choice(["ACGT", "ACDEFGHIKLMNPQRSTVWY"])
+        words = ["".join(rng.choice(alpha) for _ in range(L)) for L in (l0, b1, b1)]
+        text = "".join(rng.choice(alpha) for _ in range(80))
+        got = struct_hits(words, text, offs, s, (e0, e1, e1), one_shift=True)
         for w, e, g in zip(words, (e0, e1, e1), got):
             assert g == sellers_hits(w, text, e), (l0, e0, b1, e1)
         done += 1

@@ -228,7 +228,7 @@ __global__ void __launch_bounds__ ( kDPThreads ) k_dp_struct1 ( const StructArgs
  * per-structure counts are those of k_dp_struct1; a sequence end flushes
  * and clears the history up to it.
  */
-template <int B, bool PK>
+template <int B, bool PK, int GE = -1>
 __global__ void __launch_bounds__ ( kDPThreads ) k_dp_struct1_hd ( const StructArgs a )
 {
     extern __shared__ uint32_t smem[];
@@ -281,8 +281,28 @@ __global__ void __launch_bounds__ ( kDPThreads ) k_dp_struct1_hd ( const StructA
     const uint32_t mA = ( ( 1u << l0 ) - 1u ) << ( L - l0 );
     const uint32_t mB = ( ( 1u << l1 ) - 1u ) << ( 2 * L - l1 );
     const uint32_t mC = ( ( 1u << l1 ) - 1u ) << ( 3 * L - l1 );
+    // GE >= 0 (e0 = e1 = GE, l0 + 2 l1 + 3 <= 32): the popc-free form.  The
+    // three rows as lanes of l0, l1, l1 bits at o0, o1, o2 with a guard bit
+    // above each, the top guard at bit 31; the guards set in the mismatch
+    // word by plane 0 of fp; GE times x = (x & (x - L)) | G clears each
+    // lane's lowest set bit, and bit g_j of t = x - L is clear exactly when
+    // lane j has at most GE mismatches.  The masks take that bit by a funnel
+    // shift per position (the multiply by 2^(31-g) moves it to bit 31 on the
+    // FMA pipe) and are complemented with the bit reversal after the block.
+    const uint32_t go0 = 32 - ( l0 + 2 * l1 + 3 ), go1 = go0 + l0 + 1, go2 = go1 + l1 + 1;
+    const uint32_t gG = ( 1u << ( go0 + l0 ) ) | ( 1u << ( go1 + l1 ) ) | ( 1u << ( go2 + l1 ) );
+    const uint32_t gnL = 0u - ( ( 1u << go0 ) | ( 1u << go1 ) | ( 1u << go2 ) );
+    const uint32_t gsh0 = one << ( 31 - ( go0 + l0 ) ), gsh1 = one << ( 31 - ( go1 + l1 ) );
     uint32_t fp[B];
-    if constexpr ( PK )
+    if constexpr ( GE >= 0 )
+    {
+#pragma unroll
+        for ( int b = 0; b < B; ++b )
+            fp[b] = ( ( w0[b] >> ( 32 - l0 ) ) << go0 ) | ( ( w1a[b] >> ( 32 - l1 ) ) << go1 ) |
+                    ( ( w1b[b] >> ( 32 - l1 ) ) << go2 );
+        fp[0] |= gG;
+    }
+    else if constexpr ( PK )
     {
 #pragma unroll
         for ( int b = 0; b < B; ++b )
@@ -314,14 +334,18 @@ __global__ void __launch_bounds__ ( kDPThreads ) k_dp_struct1_hd ( const StructA
     {
         uint32_t cur[B];
         const uint32_t * win = s_win[( kb - ch.warm ) & 1];
-        if constexpr ( PK )
+        if constexpr ( PK || GE >= 0 )
         {
             uint32_t * w = s_win[( kb - ch.warm ) & 1];
             for ( uint32_t i = threadIdx.x; i < 32u * B; i += kDPThreads )
             {
                 const uint32_t b = i >> 5, r = i & 31u;
                 const uint32_t pw = __ldg ( planes + ( size_t ) b * stride + kb ), cw = __ldg ( planes + ( size_t ) b * stride + kb + 1 );
-                w[i] = ( __funnelshift_rc ( pw, cw, r + 1 ) >> ( 32 - L ) ) * rep3;
+                const uint32_t W = __funnelshift_rc ( pw, cw, r + 1 );          // newest symbol at bit 31
+                if constexpr ( GE >= 0 )
+                    w[i] = ( ( W >> ( 32 - l0 ) ) << go0 ) | ( ( W >> ( 32 - l1 ) ) << go1 ) | ( ( W >> ( 32 - l1 ) ) << go2 );
+                else
+                    w[i] = ( W >> ( 32 - L ) ) * rep3;
             }
             __syncthreads ();
         }
@@ -339,7 +363,19 @@ __global__ void __launch_bounds__ ( kDPThreads ) k_dp_struct1_hd ( const StructA
         for ( int r = 0; r < 32; ++r )
         {
             uint32_t Y[B];
-            if constexpr ( PK )
+            if constexpr ( GE >= 0 )
+            {
+                uint32_t x = 0;
+#pragma unroll
+                for ( int b = 0; b < B; ++b ) x |= fp[b] ^ win[b * 32 + r];
+#pragma unroll
+                for ( int c = 0; c < GE; ++c ) x = ( x & ( x * one + gnL ) ) | gG;
+                const uint32_t t = x * one + gnL;
+                m0 = __funnelshift_l ( t * gsh0, m0, 1 );
+                ma = __funnelshift_l ( t * gsh1, ma, 1 );
+                mb = __funnelshift_l ( t, mb, 1 );                // lane 2's guard is bit 31
+            }
+            else if constexpr ( PK )
             {
                 uint32_t x = 0;
 #pragma unroll
@@ -356,6 +392,12 @@ __global__ void __launch_bounds__ ( kDPThreads ) k_dp_struct1_hd ( const StructA
                 ma = ma * two + hd_hitbit<B> ( w1a, Y, top1, one, ne1 );
                 mb = mb * two + hd_hitbit<B> ( w1b, Y, top1, one, ne1 );
             }
+        }
+        if constexpr ( GE >= 0 )
+        {
+            m0 = ~m0;                                   // a set guard bit is a miss
+            ma = ~ma;
+            mb = ~mb;
         }
         m0 = __brev ( m0 );
         ma = __brev ( ma );
@@ -832,6 +874,18 @@ static void launch_struct_b ( const StructArgs & a, bool ed, dim3 grid, size_t s
     }
     else if ( ed )
         k_dp_struct1<B, true><<<grid, kDPThreads, smem, st>>> ( a );
+    else if ( block && a.e0 == a.e1 && a.e0 <= 3 && a.l0 + 2 * a.l1 + 3 <= 32 && ! getenv ( "MOTEX_STRUCT_NO_PACK" ) &&
+              ! getenv ( "MOTEX_STRUCT_NO_CLEAR" ) )
+    {
+        // popc-free guarded lanes (equal errors in both boxes)
+        switch ( a.e0 )
+        {
+            case 0: k_dp_struct1_hd<B, true, 0><<<grid, kDPThreads, smem, st>>> ( a ); break;
+            case 1: k_dp_struct1_hd<B, true, 1><<<grid, kDPThreads, smem, st>>> ( a ); break;
+            case 2: k_dp_struct1_hd<B, true, 2><<<grid, kDPThreads, smem, st>>> ( a ); break;
+            default: k_dp_struct1_hd<B, true, 3><<<grid, kDPThreads, smem, st>>> ( a ); break;
+        }
+    }
     else if ( block && 3 * std::max ( a.l0, a.l1 ) <= 32 && ! getenv ( "MOTEX_STRUCT_NO_PACK" ) )
         k_dp_struct1_hd<B, true><<<grid, kDPThreads, smem, st>>> ( a );
     else if ( block )

@@ -413,3 +413,85 @@ def test_structured_field_condition_is_needed():
     text = "A" * 12 + "C" * 20
     got = struct_hits(words, text, offs, s, es)
     assert any(g != sellers_hits(w, text, e) for w, e, g in zip(words, es, got))
+
+
+# ---------------------- one-gap structured Hamming: guarded lanes, bit clears
+
+def brev32(x):
+    return int(f"{x & M32:032b}"[::-1], 2)
+
+
+def struct_hd_guarded_block(words, e, text, k0, codes, nbits):
+    """k_dp_struct1_hd's guarded-lane form (GE = e) restated for the 32
+    positions k0 .. k0+31 of text: box 0 (l0 symbols) and the two box-1 rows
+    (b1 symbols each) as lanes at o0 = 32 - (l0 + 2 b1 + 3), o1, o2 with a
+    guard bit above each (the top one at bit 31); the text window's newest
+    l_j symbols copied into lane j; e clears of each lane's lowest set bit,
+    t = x - L, and lane j's mask bit = bit g_j of t, shifted in by a funnel
+    shift per position; after the block the masks are complemented and
+    bit-reversed (bit r = a hit ending at position k0 + r)."""
+    l0, b1 = len(words[0]), len(words[1])
+    o0 = 32 - (l0 + 2 * b1 + 3)
+    offs = (o0, o0 + l0 + 1, o0 + l0 + b1 + 2)
+    lens = (l0, b1, b1)
+    gs = tuple(o + l for o, l in zip(offs, lens))
+    assert gs[2] == 31
+    G = sum(1 << g for g in gs)
+    L = sum(1 << o for o in offs)
+    fp = [0] * nbits
+    for w, o, ln in zip(words, offs, lens):
+        for q, ch in enumerate(w):
+            for b in range(nbits):
+                if (codes[ch] >> b) & 1:
+                    fp[b] |= 1 << (o + q)
+    fp[0] |= G
+    m = [0, 0, 0]
+    for r in range(32):
+        k = k0 + r
+        x = 0
+        for b in range(nbits):
+            W = 0                                          # newest symbol at bit 31
+            for d in range(32):
+                if k - d >= 0 and (codes[text[k - d]] >> b) & 1:
+                    W |= 1 << (31 - d)
+            Y = 0
+            for o, ln in zip(offs, lens):
+                Y |= (W >> (32 - ln)) << o
+            x |= fp[b] ^ Y
+        for _ in range(e):
+            x = ((x & ((x - L) & M32)) | G) & M32
+        t = (x - L) & M32
+        for j, g in enumerate(gs):
+            m[j] = ((m[j] << 1) | (((t * (1 << (31 - g))) & M32) >> 31)) & M32
+    return [brev32(~mj & M32) for mj in m]
+
+
+@pytest.mark.parametrize("seed", range(12))
+def test_struct_hd_guarded_lanes_match(seed):
+    rng = random.Random(800 + seed)
+    while True:
+        l0, b1 = rng.randint(2, 12), rng.randint(2, 12)
+        if l0 + 2 * b1 + 3 <= 32:
+            break
+    e = rng.randint(0, min(3, min(l0, b1) - 1))
+    alpha = rng.choice(["ACGT", "ACDEFGHIKLMNPQRSTVWY"])
+    codes = {c: i for i, c in enumerate(sorted(set(alpha)))}
+    nbits = max(1, (len(codes) - 1).bit_length())
+    words = ["".join(rng.choice(alpha) for _ in range(n)) for n in (l0, b1, b1)]
+    text = "".join(rng.choice(alpha) for _ in range(96))
+    for w in words:                                    # plant near-occurrences
+        a = rng.randint(0, len(text) - len(w))
+        occ = list(w)
+        for q in rng.sample(range(len(w)), rng.randint(0, e)):
+            occ[q] = rng.choice(alpha)
+        text = text[:a] + "".join(occ) + text[a + len(w):]
+    for k0 in (32, 64):
+        got = struct_hd_guarded_block(words, e, text, k0, codes, nbits)
+        for j, w in enumerate(words):
+            ln = len(w)
+            want = 0
+            for r in range(32):
+                k = k0 + r
+                if sum(a != b for a, b in zip(w, text[k - ln + 1:k + 1])) <= e:
+                    want |= 1 << r
+            assert got[j] == want, (seed, j, l0, b1, e)

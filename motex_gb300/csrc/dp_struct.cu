@@ -356,8 +356,9 @@ __global__ void __launch_bounds__ ( kDPThreads ) k_dp_struct1_hd ( const StructA
         }
         const uint32_t vm = __ldg ( a.text.vmask + kb ), em = __ldg ( a.text.emask + kb );
         const bool counting = kb >= ch.begin;
-        // hit masks built in reverse bit order (position r at bit 31-r) as
-        // m * 2 + hit, multiply-adds on the FMA pipe; one bit reversal per block
+        // hit masks built in reverse bit order (position r at bit 31-r): the
+        // hit is the sign bit of a multiply-add and enters the mask by one
+        // funnel shift (m << 1 | bit 31 of the word); one bit reversal per block
         uint32_t m0 = 0, ma = 0, mb = 0;
 #pragma unroll 8
         for ( int r = 0; r < 32; ++r )
@@ -380,9 +381,9 @@ __global__ void __launch_bounds__ ( kDPThreads ) k_dp_struct1_hd ( const StructA
                 uint32_t x = 0;
 #pragma unroll
                 for ( int b = 0; b < B; ++b ) x |= fp[b] ^ win[b * 32 + r];
-                m0 = m0 * two + ( ( __popc ( x & mA ) * one + ne0 ) >> 31 );
-                ma = ma * two + ( ( __popc ( x & mB ) * one + ne1 ) >> 31 );
-                mb = mb * two + ( ( __popc ( x & mC ) * one + ne1 ) >> 31 );
+                m0 = __funnelshift_l ( __popc ( x & mA ) * one + ne0, m0, 1 );
+                ma = __funnelshift_l ( __popc ( x & mB ) * one + ne1, ma, 1 );
+                mb = __funnelshift_l ( __popc ( x & mC ) * one + ne1, mb, 1 );
             }
             else
             {
@@ -744,9 +745,9 @@ __global__ void __launch_bounds__ ( kDPThreads ) k_dp_struct1_swar_blk ( const S
         __syncwarp ();
         const uint32_t vm = __ldg ( a.text.vmask + kb ), em = __ldg ( a.text.emask + kb );
         const bool counting = kb >= ch.begin;
-        // hit masks built in reverse bit order (position r at bit 31-r) as
-        // m * 2 + hit; adds, left shifts and the hit-bit extraction are
-        // multiply-adds (FMA pipe), the logic ops of the step fill the ALU
+        // hit masks built in reverse bit order (position r at bit 31-r): adds
+        // and left shifts are multiply-adds (FMA pipe), each row's hit bit the
+        // sign of a multiply-add, appended by one funnel shift
         uint32_t m0 = 0, ma = 0, mb = 0;
         auto step = [&] ( int r ) {
             const uint32_t Eq = my_eq[rows[r]];
@@ -773,9 +774,9 @@ __global__ void __launch_bounds__ ( kDPThreads ) k_dp_struct1_swar_blk ( const S
             const uint32_t Ph2 = Ph * C.two, Mh2 = Mhs * C.two;
             Pv = Mh2 | ~( Xv | Ph2 );
             Mv = Ph2 & Xv & C.NG;
-            m0 = m0 * C.two + ( ( sc * C.nmA + C.nmA ) >> 31 );
-            ma = ma * C.two + ( ( sc * C.nmB + C.nmB ) >> 31 );
-            mb = mb * C.two + ( ( sc * C.nmC + C.nmC ) >> 31 );
+            m0 = __funnelshift_l ( sc * C.nmA + C.nmA, m0, 1 );
+            ma = __funnelshift_l ( sc * C.nmB + C.nmB, ma, 1 );
+            mb = __funnelshift_l ( sc * C.nmC + C.nmC, mb, 1 );
         };
         if ( em == 0u )
         {

@@ -204,8 +204,9 @@ __global__ void __launch_bounds__ ( kDPThreads ) k_dp_structN_blk ( const Struct
                     rows[lane] = c * kDPThreads;
                 }
                 __syncwarp ();
-                // masks built in reverse bit order (position r at bit 31-r) as
-                // m * 2 + hit; adds, left shifts and hit bits are multiply-adds
+                // masks built in reverse bit order (position r at bit 31-r); adds
+                // and left shifts are multiply-adds, each hit the sign bit of one,
+                // appended by a funnel shift
                 auto step = [&] ( int r ) {
                     const uint32_t Eq = my_eq[rows[r]];
                     const uint32_t Xv = Eq | Mv;
@@ -231,7 +232,7 @@ __global__ void __launch_bounds__ ( kDPThreads ) k_dp_structN_blk ( const Struct
                     Pv = Mh2 | ~( Xv | Ph2 );
                     Mv = Ph2 & Xv & C.NG;
 #pragma unroll
-                    for ( int b = 0; b < NR; ++b ) m[b] = m[b] * C.two + ( ( sc * C.nm[b] + C.nm[b] ) >> 31 );
+                    for ( int b = 0; b < NR; ++b ) m[b] = __funnelshift_l ( sc * C.nm[b] + C.nm[b], m[b], 1 );
                 };
                 if ( em == 0u )
                 {
@@ -276,7 +277,7 @@ __global__ void __launch_bounds__ ( kDPThreads ) k_dp_structN_blk ( const Struct
                     for ( int pl = 0; pl < B; ++pl ) x |= fp[pl] ^ wsm[pl * 32 + r];
 #pragma unroll
                     for ( int b = 0; b < NR; ++b )
-                        m[b] = m[b] * C.two + ( ( __popc ( x & C.hmask[b] ) * C.one + C.ne[b] ) >> 31 );
+                        m[b] = __funnelshift_l ( __popc ( x & C.hmask[b] ) * C.one + C.ne[b], m[b], 1 );
                 }
             }
 #pragma unroll

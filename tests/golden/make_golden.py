@@ -277,6 +277,18 @@ def cases():
     out.append(("struct9_gaps_ed", planted_boxes(28, 10, 200, 1, 5, 0, gaps9), [], None))
     many = ((0, 7, 6, 1), (0, 7, 6, 1))                                # 2 gaps, 64 structures
     out.append(("struct2_64structs_ed", planted_boxes(29, 10, 220, 1, 6, 1, many), [], None))
+    # popc-free Hamming: three guarded lanes (k 8, e 3), two lanes at the
+    # smallest k (5, e 0), and 5-mers with 3 mismatches, which hit at nearly
+    # every position (full 6-bit count fields per 32-position block)
+    w = W.dna_ed(seed=30, scale=0.01, d=0)
+    w.k, w.e, w.q = 8, 3, 40
+    out.append(("dna_hd_k8_e3", w, [], None))
+    w = W.dna_ed(seed=31, scale=0.01, d=0)
+    w.k, w.e, w.q = 5, 0, 30
+    out.append(("dna_hd_k5_e0", w, [], None))
+    w = W.dna_ed(seed=32, scale=0.006, d=0)
+    w.k, w.e, w.q = 5, 3, 30
+    out.append(("short_factor_k5_e3_dna_hd", w, [], None))
     return out
 
 

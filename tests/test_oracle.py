@@ -57,7 +57,8 @@ def test_golden_set_is_complete():
     for needed in ("dna_hd_64x500", "dna_ed_24seq", "prot_hd_20seq", "prot_ed_20seq", "struct_planted_hd",
                    "struct_planted_ed", "quorum_boundary_q29", "dna_with_N_ed", "short_seqs_ed",
                    "long_factor_k70_ed", "q0_n0_all_words", "caps_Q60_n2_N40", "struct3_box40_ed",
-                   "struct3_box40_hd", "struct_l40_ed", "struct9_gaps_ed", "struct2_64structs_ed"):
+                   "struct3_box40_hd", "struct_l40_ed", "struct9_gaps_ed", "struct2_64structs_ed",
+                   "dna_hd_k8_e3", "dna_hd_k5_e0", "short_factor_k5_e3_dna_hd"):
         assert needed in names
     assert {"bg_dna_hd_smile", "bg_prot_ed", "bg_struct_hd_smile", "bg_struct2_ed", "fore_dna_hd",
             "fore_prot_ed"} <= set(mode_cases())

@@ -51,3 +51,19 @@ def test_reference_arm_line(monkeypatch):
     assert {k: v for k, v in cfg.items() if k != "l2"} == {k: v for k, v in gpu_cfg.items() if k != "l2"}
     assert line["e2e"]["value"] == line["value"] == line["cpu_baseline"]["value"]
     assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["e2e"]["d2h_bytes_per_step"] == 0
+
+
+def test_kernel_names_follow_the_tuned_form():
+    """The bench line names the DP kernel the engine runs: the default for the
+    workload, or the form of the autotuner's entry (a negative lane count is
+    the popc-free Hamming form)."""
+    ed = W.dna_ed(scale=0.01)
+    hd_small = W.dna_hd_small(scale=0.1)
+    prot_hd = W.prot_uneven(d=0, scale=0.01)
+    assert bench.dp_kernel_name(ed) == "k_dp_swar_ed (NL=2)"
+    assert bench.dp_kernel_name(hd_small) == "k_dp_hclr (NL=2)"          # k 12: two lanes
+    assert bench.dp_kernel_name(prot_hd) == "k_dp_hclr (NL=3)"           # k 10: three lanes
+    assert bench.tuned_kernel_name(prot_hd, (8, -3, 4)) == "k_dp_hclr (NL=3) W=8 NL=3 UR=4"
+    assert bench.tuned_kernel_name(prot_hd, (8, 3, 4)) == "k_dp_hswar (NL=3) W=8 NL=3 UR=4"
+    assert bench.tuned_kernel_name(hd_small, (4, 1, 8)) == "k_dp_fast W=4 NL=1 UR=8"
+    assert bench.tuned_kernel_name(ed, (8, 2, 4)) == "k_dp_swar_ed (NL=2) W=8 NL=2 UR=4"
